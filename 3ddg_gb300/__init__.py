@@ -1,0 +1,263 @@
+"""dg3d on GB300: Python binding of the C ABI in include/dg3d.h.
+
+The product is libdg3d.so (CUDA kernels for sm_103a plus the C++ host code);
+this module only loads it with ctypes and mirrors its entry points for tests,
+benchmarks and scripting.  There is no fallback: if the library is missing or
+a call fails, a ``DGError`` is raised.
+
+The package directory name starts with a digit, so import it with
+``importlib.import_module("3ddg_gb300")``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libdg3d.so")
+
+DG_PRECISION_FP64 = 64
+DG_PRECISION_FP32 = 32
+
+
+class DGError(RuntimeError):
+    pass
+
+
+class DgParams(C.Structure):
+    """ctypes mirror of ``dg_params`` (include/dg3d.h)."""
+    _fields_ = [
+        ("order", C.c_int),
+        ("num_blocks", C.c_int * 3),
+        ("num_elements", C.c_int * 3),
+        ("elem_width", C.c_double * 3),
+        ("corner", C.c_double * 3),
+        ("rho0", C.c_double),
+        ("c0", C.c_double),
+        ("b_over_a", C.c_double),
+        ("diff_const", C.c_double),
+        ("eval_advect", C.c_int),
+        ("eval_diff", C.c_int),
+        ("eval_sponge", C.c_int),
+        ("periodic", C.c_int * 3),
+        ("sigma_max", C.c_double),
+        ("sponge_width", C.c_int * 6),
+        ("ic_gauss", C.c_int * 3),
+        ("ic_drho_amp", C.c_double),
+        ("ic_v_amp", C.c_double * 3),
+        ("ic_sigma", C.c_double),
+        ("ic_center", C.c_double * 3),
+        ("precision", C.c_int),
+        ("rk_exact", C.c_int),
+        ("lumped_mass", C.c_int),
+        ("src_face", C.c_int),
+        ("src_amp", C.c_double),
+        ("src_freq", C.c_double),
+        ("src_cycles", C.c_double),
+        ("src_phase", C.c_double),
+        ("src_radius", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load libdg3d.so (built by ``build.py``); raise if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise DGError("libdg3d.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp, i, d, cp = C.c_void_p, C.c_int, C.c_double, C.c_char_p
+        sig = {
+            "dg_params_default": (i, [C.POINTER(DgParams)]),
+            "dg_params_parse": (i, [cp, C.POINTER(DgParams), C.POINTER(d), C.POINTER(i), C.POINTER(i),
+                                    C.POINTER(i), C.POINTER(i), cp]),
+            "dg_create": (i, [C.POINTER(DgParams), cp, cp, C.POINTER(vp)]),
+            "dg_destroy": (i, [vp]),
+            "dg_step": (i, [vp, d, i]),
+            "dg_synchronize": (i, [vp]),
+            "dg_dims": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
+            "dg_get_state": (i, [vp, vp, vp]),
+            "dg_set_state": (i, [vp, vp, vp]),
+            "dg_eval_rhs": (i, [vp, vp, vp]),
+            "dg_get_grid": (i, [vp, vp, vp]),
+            "dg_time": (d, [vp]),
+            "dg_write_snapshot": (i, [vp, cp, i, i]),
+            "dg_launch_count": (C.c_longlong, [vp]),
+            "dg_state_device": (i, [vp, C.POINTER(vp), C.POINTER(C.c_size_t), C.POINTER(i)]),
+            "dg_last_error": (cp, []),
+            "dg_write_basis_files": (i, [cp, i, i]),
+            "dg_line_operators": (i, [i, i, cp, cp, vp, vp, vp, vp, vp, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = lib().dg_last_error().decode()
+        raise DGError("%s failed (%d): %s" % (what, rc, msg))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _b(s):
+    return None if s is None else os.fsencode(s)
+
+
+# Parameter-file keys (the reference's names) -> dg_params fields.
+def params_from_dict(cfg: dict) -> DgParams:
+    p = DgParams()
+    _check(lib().dg_params_default(C.byref(p)), "dg_params_default")
+
+    def seq(key, field, conv, n):
+        if key in cfg:
+            vals = cfg[key]
+            getattr(p, field)[:] = [conv(v) for v in vals][:n]
+
+    if "ORDER" in cfg:
+        p.order = int(cfg["ORDER"])
+    seq("NUM_BLOCKS", "num_blocks", int, 3)
+    seq("NUM_ELEMENTS", "num_elements", int, 3)
+    seq("ELEMENT_WIDTH", "elem_width", float, 3)
+    seq("STARTING_CORNER", "corner", float, 3)
+    for key, field in [("RHO0", "rho0"), ("C0", "c0"), ("B_OVER_A", "b_over_a"), ("DIFF_CONST", "diff_const"),
+                       ("BC_SIGMA_MAX", "sigma_max"), ("IC_DRHO_AMPLITUDE", "ic_drho_amp"),
+                       ("IC_SIGMA", "ic_sigma"), ("SRC_AMPLITUDE", "src_amp"), ("SRC_FREQUENCY", "src_freq"),
+                       ("SRC_CYCLES", "src_cycles"), ("SRC_PHASE", "src_phase"), ("SRC_RADIUS", "src_radius")]:
+        if key in cfg:
+            setattr(p, field, float(cfg[key]))
+    for key, field in [("EVALUATE_ADVECTION", "eval_advect"), ("EVALUATE_DIFFUSION", "eval_diff"),
+                       ("EVALUATE_SPONGE", "eval_sponge"), ("PRECISION", "precision"), ("RK_EXACT", "rk_exact"),
+                       ("LUMPED_MASS", "lumped_mass"), ("SRC_FACE", "src_face")]:
+        if key in cfg:
+            setattr(p, field, int(cfg[key]))
+    seq("BC_IS_PERIODIC", "periodic", int, 3)
+    seq("BC_SPONGE_WIDTH", "sponge_width", int, 6)
+    for a, k in enumerate(("IC_X_GAUSS", "IC_Y_GAUSS", "IC_Z_GAUSS")):
+        if k in cfg:
+            p.ic_gauss[a] = int(cfg[k])
+    for a, k in enumerate(("IC_VX_AMPLITUDE", "IC_VY_AMPLITUDE", "IC_VZ_AMPLITUDE")):
+        if k in cfg:
+            p.ic_v_amp[a] = float(cfg[k])
+    for a, k in enumerate(("IC_CENTER_X", "IC_CENTER_Y", "IC_CENTER_Z")):
+        if k in cfg:
+            p.ic_center[a] = float(cfg[k])
+    return p
+
+
+def parse_params(path: str, log_path: str | None = None):
+    """Parse a reference parameter file; returns (DgParams, driver dict)."""
+    p = DgParams()
+    _check(lib().dg_params_default(C.byref(p)), "dg_params_default")
+    dt = C.c_double(0.001)
+    ns, no, ft, bf = C.c_int(1), C.c_int(1), C.c_int(1), C.c_int(1)
+    _check(lib().dg_params_parse(_b(path), C.byref(p), C.byref(dt), C.byref(ns), C.byref(no), C.byref(ft),
+                                 C.byref(bf), _b(log_path)), "dg_params_parse")
+    return p, dict(DT=dt.value, NUM_TIME_SUBSTEPS=ns.value, NUM_OUTSTEPS=no.value, FREQ_TERMINAL=ft.value,
+                   BOOL_FILE=bf.value)
+
+
+class Solver:
+    """One simulation on the GPU (a handle of the C ABI)."""
+
+    def __init__(self, params, matrix_file: str | None = None, coeff_file: str | None = None):
+        if isinstance(params, dict):
+            params = params_from_dict(params)
+        self.params = params
+        h = C.c_void_p()
+        _check(lib().dg_create(C.byref(params), _b(matrix_file), _b(coeff_file), C.byref(h)), "dg_create")
+        self.h = h
+        X, Y, Z = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().dg_dims(self.h, C.byref(X), C.byref(Y), C.byref(Z)), "dg_dims")
+        self.dims = (X.value, Y.value, Z.value)
+
+    h = None
+
+    def close(self):
+        if self.h:
+            lib().dg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def step(self, dt: float, nsteps: int = 1):
+        _check(lib().dg_step(self.h, float(dt), int(nsteps)), "dg_step")
+
+    def synchronize(self):
+        _check(lib().dg_synchronize(self.h), "dg_synchronize")
+
+    def state(self, rho=None, vel=None):
+        rho = np.empty(self.dims) if rho is None else rho
+        vel = np.empty((3,) + self.dims) if vel is None else vel
+        _check(lib().dg_get_state(self.h, _ptr(rho), _ptr(vel)), "dg_get_state")
+        return rho, vel
+
+    def set_state(self, rho, vel):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        _check(lib().dg_set_state(self.h, _ptr(rho), _ptr(vel)), "dg_set_state")
+
+    def rhs(self):
+        rho = np.empty(self.dims)
+        vel = np.empty((3,) + self.dims)
+        _check(lib().dg_eval_rhs(self.h, _ptr(rho), _ptr(vel)), "dg_eval_rhs")
+        return rho, vel
+
+    def grid(self):
+        c = np.empty((3,) + self.dims)
+        s = np.empty(self.dims)
+        _check(lib().dg_get_grid(self.h, _ptr(c), _ptr(s)), "dg_get_grid")
+        return c, s
+
+    @property
+    def time(self) -> float:
+        return lib().dg_time(self.h)
+
+    @property
+    def launches(self) -> int:
+        return lib().dg_launch_count(self.h)
+
+    def write_snapshot(self, folder: str, ts: int, grid: bool = False):
+        _check(lib().dg_write_snapshot(self.h, _b(folder), int(ts), int(grid)), "dg_write_snapshot")
+
+    def device_state(self):
+        base = (C.c_void_p * 4)()
+        ns = C.c_size_t()
+        ne = C.c_int()
+        _check(lib().dg_state_device(self.h, base, C.byref(ns), C.byref(ne)), "dg_state_device")
+        return [base[i] for i in range(4)], ns.value, ne.value
+
+
+def line_operators(order: int, lumped: bool = False, matrix_file=None, coeff_file=None):
+    K = order + 1
+    out = {k: np.empty((K, K)) for k in ("mass", "stiff", "deriv")}
+    out.update({k: np.empty(K) for k in ("lift0", "liftN", "zeros")})
+    _check(lib().dg_line_operators(order, int(lumped), _b(matrix_file), _b(coeff_file), _ptr(out["mass"]),
+                                   _ptr(out["stiff"]), _ptr(out["deriv"]), _ptr(out["lift0"]),
+                                   _ptr(out["liftN"]), _ptr(out["zeros"])), "dg_line_operators")
+    return out
+
+
+def write_basis_files(folder: str, kmax: int = 10, lumped: bool = False):
+    _check(lib().dg_write_basis_files(_b(folder), kmax, int(lumped)), "dg_write_basis_files")

@@ -1,0 +1,564 @@
+// libdg3d: the C ABI of include/dg3d.h.  Owns the device buffers of one
+// simulation, issues the stage kernels of dg_kernels.cuh on its own stream and
+// moves state between host and device only on request.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "basis.h"
+#include "dg3d.h"
+#include "dg_kernels.cuh"
+#include "mesh.h"
+#include "solver_internal.h"
+
+namespace dg {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define DG_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t _e = (call);                                                               \
+        if (_e != cudaSuccess)                                                                 \
+            return fail(DG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));    \
+    } while (0)
+
+double burst_pressure(const dg_params& p, double t)
+{
+    if (p.src_face < 0) return 0.0;
+    const double T = p.src_cycles / p.src_freq;
+    if (t < 0.0 || t > T) return 0.0;
+    const double w = std::sin(M_PI * t / T);
+    return p.src_amp * w * w * std::sin(2.0 * M_PI * p.src_freq * t + p.src_phase);
+}
+
+namespace {
+
+template <typename T, int K>
+OpConst<T, K> make_const(const dg_params& p, const LineOperators& op)
+{
+    OpConst<T, K> C;
+    std::memset(&C, 0, sizeof C);
+    for (int i = 0; i < K; i++) {
+        for (int j = 0; j < K; j++) C.D[i][j] = (T)op.deriv[i * K + j];
+        C.L0[i] = (T)op.lift0[i];
+        C.LN[i] = (T)op.liftN[i];
+    }
+    const double r0 = p.rho0, c0 = p.c0;
+    for (int a = 0; a < 3; a++) {
+        const double w = p.elem_width[a];
+        C.inv_w[a] = (T)(1.0 / w);
+        C.s_mom[a] = (T)(-1.0 / (r0 * w));
+        C.s_mass[a] = (T)(-r0 / w);
+        C.s_diff[a] = (T)(-p.diff_const / w);
+    }
+    // Face-flux coefficients exactly as cppsrc/Element.cpp:542-556 (left) and
+    // :581-595 (right) form them; z = rho0 c0 and r = rho0 on both sides.
+    const double z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
+    const double cL0[4] = {z1 * r2 / (z1 + z2), z2 * r1 / (z1 + z2), z1 * z2 / r2 / (z1 + z2),
+                           -1.0 * z1 * z2 / r1 / (z1 + z2)};
+    const double cL1[4] = {z2 / r2 / (z1 + z2), z1 / r1 / (z1 + z2), r2 / (z1 + z2), -1.0 * r1 / (z1 + z2)};
+    const double cR0[4] = {z2 * r1 / (z1 + z2), z1 * r2 / (z1 + z2), z1 * z2 / r1 / (z1 + z2),
+                           -1.0 * z1 * z2 / r2 / (z1 + z2)};
+    const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
+    for (int i = 0; i < 4; i++) {
+        C.cL0[i] = (T)cL0[i];
+        C.cL1[i] = (T)cL1[i];
+        C.cR0[i] = (T)cR0[i];
+        C.cR1[i] = (T)cR1[i];
+    }
+    C.ba = (T)p.b_over_a;
+    C.inv_r0 = (T)(1.0 / r0);
+    C.c2_r0 = (T)(c0 * c0 / r0);
+    C.r0 = (T)r0;
+    C.inv_c2 = (T)(1.0 / (c0 * c0));
+    C.inv_z = (T)(1.0 / (r0 * c0));
+    C.linear_mass = p.b_over_a == 0.0 ? 1 : 0;
+    bool diag = true;
+    for (int i = 0; i < K; i++)
+        for (int j = 0; j < K; j++)
+            if (i != j && op.mass[i * K + j] != 0.0) diag = false;
+    C.dense_lift = diag ? 0 : 1;
+    return C;
+}
+
+template <typename T, int K, bool INCR>
+void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+{
+    const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
+    dim3 block(npt_of(K), epb_of(K));
+    dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
+    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, C);
+    s.launches++;
+}
+
+template <typename T, int K, bool INCR>
+void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+{
+    const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
+    dim3 block(npt_of(K), epb_of(K));
+    dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
+    if (s.p.eval_diff)
+        stage_kernel<T, K, true, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
+    else
+        stage_kernel<T, K, false, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
+    s.launches++;
+}
+
+template <typename T, bool INCR>
+void dispatch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+{
+    switch (s.mesh.K) {
+    case 2: launch_grad<T, 2, INCR>(s, io, md); break;
+    case 3: launch_grad<T, 3, INCR>(s, io, md); break;
+    case 4: launch_grad<T, 4, INCR>(s, io, md); break;
+    case 5: launch_grad<T, 5, INCR>(s, io, md); break;
+    case 6: launch_grad<T, 6, INCR>(s, io, md); break;
+    case 7: launch_grad<T, 7, INCR>(s, io, md); break;
+    case 8: launch_grad<T, 8, INCR>(s, io, md); break;
+    }
+}
+
+template <typename T, bool INCR>
+void dispatch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+{
+    switch (s.mesh.K) {
+    case 2: launch_stage<T, 2, INCR>(s, io, md); break;
+    case 3: launch_stage<T, 3, INCR>(s, io, md); break;
+    case 4: launch_stage<T, 4, INCR>(s, io, md); break;
+    case 5: launch_stage<T, 5, INCR>(s, io, md); break;
+    case 6: launch_stage<T, 6, INCR>(s, io, md); break;
+    case 7: launch_stage<T, 7, INCR>(s, io, md); break;
+    case 8: launch_stage<T, 8, INCR>(s, io, md); break;
+    }
+}
+
+template <typename T>
+MeshDev<T> mesh_dev(const Solver& s)
+{
+    MeshDev<T> m;
+    m.nbr = s.d_nbr;
+    m.sigma = (const T*)s.d_sigma;
+    m.bnd_ic = (const T*)s.d_bnd_ic;
+    m.bnd_ap = (const T*)s.d_bnd_ap;
+    m.bnd_src = s.d_bnd_src;
+    m.n_elem = s.mesh.n_elem;
+    m.ic_live = 0;
+    m.src_p = T(0);
+    return m;
+}
+
+template <typename T>
+int upload_as(const std::vector<double>& h, void** d)
+{
+    std::vector<T> tmp(h.begin(), h.end());
+    size_t bytes = std::max<size_t>(tmp.size(), 1) * sizeof(T);
+    DG_CUDA(cudaMalloc(d, bytes));
+    if (!tmp.empty()) DG_CUDA(cudaMemcpy(*d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return DG_OK;
+}
+
+GridMap grid_map(const MeshHost& m)
+{
+    GridMap g;
+    g.K = m.K;
+    for (int a = 0; a < 3; a++) {
+        g.nb[a] = m.nb[a];
+        g.ne[a] = m.ne[a];
+        g.E[a] = m.E[a];
+    }
+    g.elem_per_block = m.elem_per_block;
+    return g;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// One RK step (three stages) in each precision.
+// ---------------------------------------------------------------------------
+int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
+{
+    MeshDev<double> md = mesh_dev<double>(*this);
+    const double w23 = p.rk_exact ? 2.0 / 3.0 : (double)(2.0f / 3.0f);
+    const double w13 = p.rk_exact ? 1.0 / 3.0 : (double)(1.0f / 3.0f);
+    const double tst[3] = {t, t + dt, t + 0.5 * dt};
+    double* U = (double*)buf[0];
+    double* k1 = (double*)buf[1];
+    double* k2 = (double*)buf[2];
+    StageIO<double> io;
+    std::memset(&io, 0, sizeof io);
+    io.fs = mesh.fstride();
+    io.np = mesh.NP;
+    io.q = (const double*)qbuf;
+    io.q_out = (double*)qbuf;
+    if (rhs_only) {
+        io.src = U;
+        io.dst = rhs_only;
+        io.ca = 1.0;
+        io.cb = 0.0;
+    } else if (s_idx == 0) {
+        io.src = U; io.dst = k1; io.old = nullptr; io.ca = dt; io.cb = 1.0; io.cc = 0.0;
+    } else if (s_idx == 1) {
+        io.src = k1; io.dst = k2; io.old = U; io.ca = dt * .25; io.cb = .25; io.cc = .75;
+    } else {
+        io.src = k2; io.dst = U; io.old = U; io.ca = dt * 2.0 / 3.0; io.cb = w23; io.cc = w13;
+    }
+    md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
+    md.src_p = burst_pressure(p, tst[s_idx]);
+    if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
+    dispatch_stage<double, false>(*this, io, md);
+    return DG_OK;
+}
+
+int Solver::rk_stage_fp32(int s_idx, double dt, float* rhs_only)
+{
+    MeshDev<float> md = mesh_dev<float>(*this);
+    const double w23 = p.rk_exact ? 2.0 / 3.0 : (double)(2.0f / 3.0f);
+    const double w13 = p.rk_exact ? 1.0 / 3.0 : (double)(1.0f / 3.0f);
+    const double tst[3] = {t, t + dt, t + 0.5 * dt};
+    float* u = (float*)buf[cur];
+    float* unext = (float*)buf[1 - cur];
+    float* comp = (float*)buf[2];
+    float* d1 = (float*)buf[3];
+    float* d2 = (float*)buf[4];
+    StageIO<float> io;
+    std::memset(&io, 0, sizeof io);
+    io.fs = mesh.fstride();
+    io.np = mesh.NP;
+    io.q = (const float*)qbuf;
+    io.q_out = (float*)qbuf;
+    io.src = u;
+    if (rhs_only) {
+        io.dst = rhs_only;
+        io.ca = 1.0f;
+    } else if (s_idx == 0) {
+        io.dst = d1;
+        io.ca = (float)dt;
+    } else if (s_idx == 1) {
+        io.inc = d1; io.dst = d2; io.ca = (float)(dt * .25); io.cb = .25f;
+    } else {
+        io.inc = d2; io.dst = unext; io.comp = comp; io.final_stage = 1;
+        io.ca = (float)(dt * 2.0 / 3.0);
+        io.cb = (float)w23;
+        io.eps = (float)(w23 + w13 - 1.0);
+    }
+    md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
+    md.src_p = (float)burst_pressure(p, tst[s_idx]);
+    if (p.eval_diff) dispatch_grad<float, true>(*this, io, md);
+    dispatch_stage<float, true>(*this, io, md);
+    return DG_OK;
+}
+
+int Solver::step(double dt, int nsteps)
+{
+    for (int n = 0; n < nsteps; n++) {
+        for (int s = 0; s < 3; s++) {
+            int rc = fp64() ? rk_stage_fp64(s, dt, nullptr) : rk_stage_fp32(s, dt, nullptr);
+            if (rc) return rc;
+        }
+        DG_CUDA(cudaGetLastError());
+        if (!fp64()) cur = 1 - cur;
+        ic_live = false;
+        t += dt;
+        steps_done++;
+    }
+    return DG_OK;
+}
+
+int Solver::eval_rhs(double* drho, double* vel)
+{
+    // R = L(current state) into the k1 / d1 buffer, then pack.
+    if (fp64()) rk_stage_fp64(0, 0.0, (double*)buf[1]);
+    else rk_stage_fp32(0, 0.0, (float*)buf[3]);
+    DG_CUDA(cudaGetLastError());
+    return pack_out(fp64() ? buf[1] : buf[3], drho, vel);
+}
+
+void* Solver::state_ptr() const { return fp64() ? buf[0] : buf[cur]; }
+
+int Solver::ensure_staging()
+{
+    if (staging) return DG_OK;
+    DG_CUDA(cudaMalloc(&staging, 4 * gsize() * sizeof(double)));
+    return DG_OK;
+}
+
+int Solver::pack_out(const void* src, double* drho, double* vel)
+{
+    int rc = ensure_staging();
+    if (rc) return rc;
+    const GridMap g = grid_map(mesh);
+    const int threads = 256;
+    const long long total = (long long)mesh.n_elem * mesh.K * mesh.K * mesh.K;
+    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 152LL * 32);
+    if (fp64())
+        pack_grid_kernel<double><<<blocks, threads, 0, stream>>>((const double*)src, mesh.fstride(), mesh.NP, 4, g,
+                                                                 mesh.n_elem, staging, gsize());
+    else
+        pack_grid_kernel<float><<<blocks, threads, 0, stream>>>((const float*)src, mesh.fstride(), mesh.NP, 4, g,
+                                                                mesh.n_elem, staging, gsize());
+    launches++;
+    DG_CUDA(cudaGetLastError());
+    if (drho) DG_CUDA(cudaMemcpyAsync(drho, staging, gsize() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (vel)
+        DG_CUDA(cudaMemcpyAsync(vel, staging + gsize(), 3 * gsize() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    DG_CUDA(cudaStreamSynchronize(stream));
+    return DG_OK;
+}
+
+int Solver::unpack_in(const double* drho, const double* vel)
+{
+    int rc = ensure_staging();
+    if (rc) return rc;
+    DG_CUDA(cudaMemcpyAsync(staging, drho, gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    DG_CUDA(cudaMemcpyAsync(staging + gsize(), vel, 3 * gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    const GridMap g = grid_map(mesh);
+    const int threads = 256;
+    const long long total = (long long)mesh.n_elem * mesh.K * mesh.K * mesh.K;
+    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 152LL * 32);
+    if (fp64())
+        unpack_grid_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(), mesh.NP, 4,
+                                                                   g, mesh.n_elem, staging, gsize());
+    else {
+        unpack_grid_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP, 4, g,
+                                                                  mesh.n_elem, staging, gsize());
+        DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
+    }
+    launches++;
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaStreamSynchronize(stream));
+    ic_live = false;
+    return DG_OK;
+}
+
+size_t Solver::device_bytes() const
+{
+    const size_t fs = mesh.fstride();
+    const size_t es = fp64() ? 8 : 4;
+    size_t nbuf = fp64() ? 3 : 5;  // FP64: U, k1, k2; FP32: u0, u1, comp, d1, d2
+    size_t bytes = nbuf * 4 * fs * es + 3 * fs * es;
+    bytes += (size_t)mesh.n_elem * 6 * sizeof(int) + (size_t)mesh.n_elem * es;
+    bytes += (size_t)mesh.n_bnd * (3 * mesh.K * mesh.K * es + sizeof(int));
+    return bytes;
+}
+
+int Solver::init(const dg_params& prm, const char* matrix_file, const char* coeff_file)
+{
+    p = prm;
+    std::string err = validate_params(p);
+    if (!err.empty()) return fail(DG_ERR_INVALID, err);
+    err = build_line_operators(p.order, p.lumped_mass != 0, matrix_file ? matrix_file : "",
+                               coeff_file ? coeff_file : "", op);
+    if (!err.empty()) return fail(err.find("Opening") == 0 ? DG_ERR_IO : DG_ERR_INVALID, err);
+    err = build_mesh(p, op, mesh);
+    if (!err.empty()) return fail(DG_ERR_INVALID, err);
+
+    DG_CUDA(cudaGetDevice(&device));
+    size_t free_b = 0, total_b = 0;
+    DG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = device_bytes();
+    if (need > free_b)
+        return fail(DG_ERR_NOMEM, "state needs " + std::to_string(need) + " bytes, device has " +
+                                      std::to_string(free_b) + " free");
+    DG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+
+    const size_t fs = mesh.fstride();
+    const size_t es = fp64() ? 8 : 4;
+    const int nbuf = fp64() ? 3 : 5;
+    for (int i = 0; i < nbuf; i++) {
+        DG_CUDA(cudaMalloc(&buf[i], 4 * fs * es));
+        DG_CUDA(cudaMemsetAsync(buf[i], 0, 4 * fs * es, stream));
+    }
+    DG_CUDA(cudaMalloc(&qbuf, 3 * fs * es));
+    DG_CUDA(cudaMemsetAsync(qbuf, 0, 3 * fs * es, stream));
+    DG_CUDA(cudaMalloc(&d_nbr, mesh.nbr.size() * sizeof(int)));
+    DG_CUDA(cudaMemcpy(d_nbr, mesh.nbr.data(), mesh.nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<int> is_src(std::max(mesh.n_bnd, 1), 0);
+    for (int b = 0; b < mesh.n_bnd; b++) is_src[b] = mesh.bnd_face[b] == p.src_face ? 1 : 0;
+    DG_CUDA(cudaMalloc(&d_bnd_src, is_src.size() * sizeof(int)));
+    DG_CUDA(cudaMemcpy(d_bnd_src, is_src.data(), is_src.size() * sizeof(int), cudaMemcpyHostToDevice));
+    int rc;
+    if (fp64()) {
+        if ((rc = upload_as<double>(mesh.sigma, &d_sigma))) return rc;
+        if ((rc = upload_as<double>(mesh.bnd_ic, &d_bnd_ic))) return rc;
+        if ((rc = upload_as<double>(mesh.bnd_ap, &d_bnd_ap))) return rc;
+        DG_CUDA(cudaMemcpy(buf[0], mesh.state0.data(), 4 * fs * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        if ((rc = upload_as<float>(mesh.sigma, &d_sigma))) return rc;
+        if ((rc = upload_as<float>(mesh.bnd_ic, &d_bnd_ic))) return rc;
+        if ((rc = upload_as<float>(mesh.bnd_ap, &d_bnd_ap))) return rc;
+        std::vector<float> s0(mesh.state0.begin(), mesh.state0.end());
+        DG_CUDA(cudaMemcpy(buf[0], s0.data(), 4 * fs * sizeof(float), cudaMemcpyHostToDevice));
+        cur = 0;
+    }
+    DG_CUDA(cudaStreamSynchronize(stream));
+    // The initial state lives on the device now; keep no host copy of it.
+    std::vector<double>().swap(mesh.state0);
+    ic_live = true;
+    t = 0.0;
+    return DG_OK;
+}
+
+Solver::~Solver()
+{
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* b : buf)
+        if (b) cudaFree(b);
+    if (qbuf) cudaFree(qbuf);
+    if (staging) cudaFree(staging);
+    if (d_nbr) cudaFree(d_nbr);
+    if (d_sigma) cudaFree(d_sigma);
+    if (d_bnd_ic) cudaFree(d_bnd_ic);
+    if (d_bnd_ap) cudaFree(d_bnd_ap);
+    if (d_bnd_src) cudaFree(d_bnd_src);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+}  // namespace dg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using dg::fail;
+using dg::Solver;
+
+extern "C" {
+
+int dg_create(const dg_params* p, const char* matrix_file, const char* coeff_file, dg_handle** out)
+{
+    if (!p || !out) return fail(DG_ERR_INVALID, "dg_create: null argument");
+    *out = nullptr;
+    dg_handle* h = new (std::nothrow) dg_handle;
+    if (!h) return fail(DG_ERR_NOMEM, "dg_create: host allocation failed");
+    int rc = h->s.init(*p, matrix_file, coeff_file);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    dg::g_last_error.clear();
+    *out = h;
+    return DG_OK;
+}
+
+int dg_destroy(dg_handle* h)
+{
+    delete h;
+    return DG_OK;
+}
+
+int dg_step(dg_handle* h, double dt, int nsteps)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_step: null handle");
+    if (nsteps < 0 || !std::isfinite(dt)) return fail(DG_ERR_INVALID, "dg_step: bad dt or nsteps");
+    return h->s.step(dt, nsteps);
+}
+
+int dg_synchronize(dg_handle* h)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_synchronize: null handle");
+    cudaError_t e = cudaStreamSynchronize(h->s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    return DG_OK;
+}
+
+int dg_dims(const dg_handle* h, int* X, int* Y, int* Z)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_dims: null handle");
+    const dg::MeshHost& m = h->s.mesh;
+    if (X) *X = m.E[0] * m.K;
+    if (Y) *Y = m.E[1] * m.K;
+    if (Z) *Z = m.E[2] * m.K;
+    return DG_OK;
+}
+
+int dg_get_state(dg_handle* h, double* drho, double* vel)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_get_state: null handle");
+    return h->s.pack_out(h->s.state_ptr(), drho, vel);
+}
+
+int dg_set_state(dg_handle* h, const double* drho, const double* vel)
+{
+    if (!h || !drho || !vel) return fail(DG_ERR_INVALID, "dg_set_state: null argument");
+    return h->s.unpack_in(drho, vel);
+}
+
+int dg_eval_rhs(dg_handle* h, double* drho, double* vel)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_eval_rhs: null handle");
+    return h->s.eval_rhs(drho, vel);
+}
+
+int dg_get_grid(dg_handle* h, double* coords, double* sigma)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_get_grid: null handle");
+    const dg::MeshHost& m = h->s.mesh;
+    const int K3 = m.K * m.K * m.K;
+    const size_t gs = h->s.gsize();
+    std::vector<double> x;
+    for (int e = 0; e < m.n_elem; e++) {
+        m.node_coords(h->s.p, h->s.op, e, x);
+        for (int n = 0; n < K3; n++) {
+            size_t g = dg::grid_offset(m, e, n);
+            if (coords)
+                for (int a = 0; a < 3; a++) coords[a * gs + g] = x[a * K3 + n];
+            if (sigma) sigma[g] = m.sigma[e];
+        }
+    }
+    return DG_OK;
+}
+
+double dg_time(const dg_handle* h) { return h ? h->s.t : 0.0; }
+
+long long dg_launch_count(const dg_handle* h) { return h ? h->s.launches : 0; }
+
+int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem)
+{
+    if (!h || !base) return fail(DG_ERR_INVALID, "dg_state_device: null argument");
+    const size_t es = h->s.fp64() ? 8 : 4;
+    char* b = (char*)h->s.state_ptr();
+    for (int f = 0; f < 4; f++) base[f] = b + (size_t)f * h->s.mesh.fstride() * es;
+    if (node_stride) *node_stride = (size_t)h->s.mesh.NP;
+    if (n_elem) *n_elem = h->s.mesh.n_elem;
+    return DG_OK;
+}
+
+const char* dg_last_error(void) { return dg::g_last_error.c_str(); }
+
+int dg_write_basis_files(const char* folder, int kmax, int lumped_mass)
+{
+    if (!folder || kmax < 2 || kmax > 10) return fail(DG_ERR_INVALID, "dg_write_basis_files: bad argument");
+    std::string err = dg::write_coeff_files(folder, kmax);
+    if (err.empty()) err = dg::write_matrix_file(std::string(folder) + "/matrices.txt", kmax - 1, lumped_mass != 0);
+    if (!err.empty()) return fail(DG_ERR_IO, err);
+    return DG_OK;
+}
+
+int dg_line_operators(int order, int lumped_mass, const char* matrix_file, const char* coeff_file, double* mass,
+                      double* stiff, double* deriv, double* lift0, double* liftN, double* zeros)
+{
+    dg::LineOperators op;
+    std::string err = dg::build_line_operators(order, lumped_mass != 0, matrix_file ? matrix_file : "",
+                                               coeff_file ? coeff_file : "", op);
+    if (!err.empty()) return fail(err.find("Opening") == 0 ? DG_ERR_IO : DG_ERR_INVALID, err);
+    const int K = order + 1;
+    if (mass) std::memcpy(mass, op.mass.data(), sizeof(double) * K * K);
+    if (stiff) std::memcpy(stiff, op.stiff.data(), sizeof(double) * K * K);
+    if (deriv) std::memcpy(deriv, op.deriv.data(), sizeof(double) * K * K);
+    if (lift0) std::memcpy(lift0, op.lift0.data(), sizeof(double) * K);
+    if (liftN) std::memcpy(liftN, op.liftN.data(), sizeof(double) * K);
+    if (zeros) std::memcpy(zeros, op.zeros.data(), sizeof(double) * K);
+    return DG_OK;
+}
+
+}  // extern "C"

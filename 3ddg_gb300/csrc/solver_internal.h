@@ -1,0 +1,63 @@
+// Internal state of one simulation handle (shared by the C-ABI translation
+// units of libdg3d; not part of the public interface).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "basis.h"
+#include "dg3d.h"
+#include "mesh.h"
+
+namespace dg {
+
+extern thread_local std::string g_last_error;
+int fail(int code, const std::string& msg);
+double burst_pressure(const dg_params& p, double t);
+
+struct Solver {
+    dg_params p{};
+    LineOperators op;
+    MeshHost mesh;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // FP64: buf[0] = U (stage 3 writes it in place), buf[1] = k1, buf[2] = k2.
+    // FP32: buf[0], buf[1] = u ping-pong (buf[cur] current), buf[2] = Kahan
+    //       compensation, buf[3] = d1, buf[4] = d2.
+    void* buf[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    void* qbuf = nullptr;       // LDG gradient, 3 fields
+    double* staging = nullptr;  // 4 node-duplicated FP64 fields for host transfers
+    int* d_nbr = nullptr;
+    void* d_sigma = nullptr;
+    void* d_bnd_ic = nullptr;
+    void* d_bnd_ap = nullptr;
+    int* d_bnd_src = nullptr;
+    int cur = 0;
+    bool ic_live = false;
+    double t = 0.0;
+    long long steps_done = 0;
+    long long launches = 0;
+
+    bool fp64() const { return p.precision == DG_PRECISION_FP64; }
+    size_t gsize() const { return (size_t)mesh.n_elem * mesh.K * mesh.K * mesh.K; }
+    size_t device_bytes() const;
+    void* state_ptr() const;
+
+    int init(const dg_params& prm, const char* matrix_file, const char* coeff_file);
+    int step(double dt, int nsteps);
+    int rk_stage_fp64(int s, double dt, double* rhs_only);
+    int rk_stage_fp32(int s, double dt, float* rhs_only);
+    int eval_rhs(double* drho, double* vel);
+    int ensure_staging();
+    int pack_out(const void* src, double* drho, double* vel);
+    int unpack_in(const double* drho, const double* vel);
+    ~Solver();
+};
+
+}  // namespace dg
+
+// The opaque handle of the C ABI.
+struct dg_handle {
+    dg::Solver s;
+};

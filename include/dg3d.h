@@ -1,0 +1,168 @@
+/* dg3d: GB300-native DG right-hand side and SSP-RK3 time loop for 3DDG.
+ *
+ * C ABI of libdg3d.so.  Plain C types only (no CUDA or C++ types), int status
+ * returns (0 = success, negative = error; dg_last_error() has the message),
+ * caller-owned host buffers, library-owned device buffers.  One handle per
+ * host thread.  All stepping is stream-ordered on the handle's CUDA stream.
+ *
+ * The reference (drewalan/3DDG) has no plugin or FFI layer: its hot path is the
+ * C++ class surface that main() drives (cppsrc/driver.cpp:199-278).  Each
+ * entry point below names the reference interface it replaces; the C++ facade
+ * classes Grid/Block/Element/Basis in this package (csrc/host/) keep the
+ * reference's signatures and call these entry points.
+ */
+#ifndef DG3D_H
+#define DG3D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DG_OK 0
+#define DG_ERR_INVALID (-1)   /* bad argument or parameter */
+#define DG_ERR_CUDA (-2)      /* CUDA runtime error */
+#define DG_ERR_NOMEM (-3)     /* device allocation refused or over budget */
+#define DG_ERR_IO (-4)        /* file could not be opened, read or written */
+#define DG_ERR_STATE (-5)     /* call not valid in the handle's current state */
+
+#define DG_PRECISION_FP64 64  /* the plain method: FP64 fields, fluxes, stages */
+#define DG_PRECISION_FP32 32  /* FP32 fields/fluxes, Kahan-compensated update */
+
+/* Simulation parameters.  Field names and meanings follow the reference's
+ * parameter file keys (parameters1.txt; parsed at cppsrc/driver.cpp:139-186),
+ * the Grid constructor arguments (cppsrc/Grid.h:33) and struct BCParam
+ * (cppsrc/BCParam.h:13-36). */
+typedef struct dg_params {
+    int order;                 /* ORDER: polynomial order N (nodes per line N+1), 1..8 */
+    int num_blocks[3];         /* NUM_BLOCKS */
+    int num_elements[3];       /* NUM_ELEMENTS, per block */
+    double elem_width[3];      /* ELEMENT_WIDTH */
+    double corner[3];          /* STARTING_CORNER */
+    double rho0;               /* RHO0 */
+    double c0;                 /* C0 */
+    double b_over_a;           /* B_OVER_A (0 selects the linear mass flux) */
+    double diff_const;         /* DIFF_CONST */
+    int eval_advect;           /* EVALUATE_ADVECTION */
+    int eval_diff;             /* EVALUATE_DIFFUSION */
+    int eval_sponge;           /* EVALUATE_SPONGE */
+    int periodic[3];           /* BC_IS_PERIODIC */
+    double sigma_max;          /* BC_SIGMA_MAX */
+    int sponge_width[6];       /* BC_SPONGE_WIDTH: -X +X -Y +Y -Z +Z */
+    int ic_gauss[3];           /* IC_X_GAUSS, IC_Y_GAUSS, IC_Z_GAUSS */
+    double ic_drho_amp;        /* IC_DRHO_AMPLITUDE */
+    double ic_v_amp[3];        /* IC_VX/VY/VZ_AMPLITUDE */
+    double ic_sigma;           /* IC_SIGMA (inverse square length) */
+    double ic_center[3];       /* IC_CENTER_X/Y/Z */
+    /* Extensions (not in the reference; defaults reproduce it): */
+    int precision;             /* DG_PRECISION_FP64 (default) or DG_PRECISION_FP32 */
+    int rk_exact;              /* 0: the reference's RK weights (its stage-3 weights
+                                  2.0F/3.0F, 1.0F/3.0F are float literals); 1: exact */
+    int lumped_mass;           /* 1: diagonal LGL mass matrix when none is read from file */
+    int src_face;              /* tone-burst source face (-X +X -Y +Y -Z +Z = 0..5), -1 none */
+    double src_amp;            /* source pressure amplitude */
+    double src_freq;           /* centre frequency */
+    double src_cycles;         /* cycles under the Hann window */
+    double src_phase;          /* phase offset, radians */
+    double src_radius;         /* aperture radius about the face centre (<= 0: whole face) */
+} dg_params;
+
+typedef struct dg_handle dg_handle;
+
+/* Fill *p with the reference's BCParam defaults (cppsrc/BCParam.cpp:24) and
+ * the driver's compiled-in defaults (cppsrc/driver.cpp:48-65). */
+int dg_params_default(dg_params* p);
+
+/* Parse a parameter file in the reference's "KEY = values" format; replaces
+ * the parser in main() (cppsrc/driver.cpp:129-196).  Keys absent from the file
+ * keep the values already in *p.  Driver-only keys are returned through the
+ * optional pointers (NULL to ignore).  If log_path is non-NULL the file is
+ * echoed there as "Parameters used:\n{\n  <line>\n}\n" like the reference's
+ * _log.txt.  Unknown keys produce the reference's warning on stderr. */
+int dg_params_parse(const char* path, dg_params* p, double* dt, int* num_substeps,
+                    int* num_outsteps, int* freq_terminal, int* bool_file,
+                    const char* log_path);
+
+/* Build the mesh, operators and initial condition and upload them; replaces
+ * Grid::Grid + Basis::Basis (cppsrc/Grid.h:33, cppsrc/Basis.h:26) and the
+ * three Grid copies the driver makes (cppsrc/driver.cpp:199-213).
+ * matrix_file / coeff_file: the reference's matrices.txt and
+ * hardcoded_coeff.txt (NULL: computed in FP64 from LGL mathematics). */
+int dg_create(const dg_params* p, const char* matrix_file, const char* coeff_file,
+              dg_handle** out);
+
+/* Release every device and host resource of the handle. */
+int dg_destroy(dg_handle* h);
+
+/* Advance nsteps SSP-RK3 steps of size dt; replaces the driver's inner loop
+ * around Grid::RK33 (cppsrc/driver.cpp:256-277, cppsrc/Grid.cpp:642-902),
+ * including Grid::communicate (cppsrc/Grid.cpp:487-565), which becomes an
+ * on-device face gather.  Asynchronous on the handle's stream. */
+int dg_step(dg_handle* h, double dt, int nsteps);
+
+/* Wait for all work queued on the handle's stream. */
+int dg_synchronize(dg_handle* h);
+
+/* Node-duplicated global dimensions X = NB_x*E_x*(N+1), Y, Z: the array shape
+ * of the reference's HDF5 datasets (cppsrc/HDF5Functions.cpp:160-168). */
+int dg_dims(const dg_handle* h, int* X, int* Y, int* Z);
+
+/* Copy the current state to host buffers: drho [X][Y][Z], vel [3][X][Y][Z]
+ * (either may be NULL).  Replaces the gather of dumpToHDF5File
+ * (cppsrc/HDF5Functions.cpp:173-208).  Synchronous. */
+int dg_get_state(dg_handle* h, double* drho, double* vel);
+
+/* Overwrite the current state from host buffers of the same layout.  Boundary
+ * exterior values become zero (no initial-condition halo).  Synchronous. */
+int dg_set_state(dg_handle* h, const double* drho, const double* vel);
+
+/* One evaluation R = L(u) of the semi-discrete right-hand side at the current
+ * state (LDG diffusion, advection, sponge; no RK combination) into host
+ * buffers of the dg_get_state layout: the per-stage operator sum that
+ * Grid::RK33 accumulates into k1 before selfWeightedAdd (cppsrc/Grid.cpp:
+ * 655-704).  The state and time are unchanged.  Synchronous. */
+int dg_eval_rhs(dg_handle* h, double* drho, double* vel);
+
+/* Node coordinates [3][X][Y][Z] and per-node sponge sigma [X][Y][Z] (either
+ * may be NULL); the data of dumpGridToHDF5File (cppsrc/HDF5Functions.cpp:34-142). */
+int dg_get_grid(dg_handle* h, double* coords, double* sigma);
+
+/* Simulation time (sum of the dt of every completed step). */
+double dg_time(const dg_handle* h);
+
+/* Write the reference's snapshot files for time step ts into folder/raw/:
+ * dRho_<b>_<ts>.h5 ("rho" [X][Y][Z] f64 + "time") and vel_<b>_<ts>.h5
+ * ("velocity" [3][X][Y][Z] + "time"), one file pair per block b like one MPI
+ * rank of the reference (cppsrc/HDF5Functions.cpp:145-247); with grid != 0
+ * also coords/ba/diff/rho0/c0 (cppsrc/HDF5Functions.cpp:34-142).  The state is
+ * copied back from the device only here.  Returns 0, or the reference's codes
+ * -1..-4 for file/dataset failures. */
+int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int grid);
+
+/* Number of kernel launches issued by this handle since creation (profiling). */
+long long dg_launch_count(const dg_handle* h);
+
+/* Device pointers of the current state fields (FP64 or FP32 per precision),
+ * element-major: field f, element e, node n at base[f] + e*node_stride + n,
+ * node n = (i*K + j)*K + k.  For zero-copy integration and benchmarking. */
+int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem);
+
+/* Last error message of this thread ("" if none). */
+const char* dg_last_error(void);
+
+/* Write hardcoded_coeff.txt, hardcoded_coeff2.txt (point counts 1..kmax) and
+ * matrices.txt (orders 1..kmax-1) into folder, in the formats the reference
+ * reads (cppsrc/Basis.cpp:74-237, cppsrc/Grid.cpp:920-989). */
+int dg_write_basis_files(const char* folder, int kmax, int lumped_mass);
+
+/* Unit-interval operators of one order as used on the device: mass, stiff,
+ * deriv (D = M^-1 S) each (N+1)^2 row-major, lift0/liftN (N+1), zeros (N+1). */
+int dg_line_operators(int order, int lumped_mass, const char* matrix_file,
+                      const char* coeff_file, double* mass, double* stiff,
+                      double* deriv, double* lift0, double* liftN, double* zeros);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DG3D_H */

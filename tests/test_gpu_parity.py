@@ -1,0 +1,158 @@
+"""GPU FP64 path against the C oracle on identical seeded inputs, through the
+C ABI.  Tolerances: one right-hand-side evaluation to 1e-12 relative (rounding
+only), multi-step runs to 1e-10 max relative pressure error."""
+import numpy as np
+import pytest
+
+from conftest import max_rel, pressure, workloads
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+STEP_TOL = 1e-10
+
+
+def small(order=3, ne=(4, 3, 5), **kw):
+    W = workloads()
+    cfg = W.gaussian_pulse(seed=1, num_elements=ne, order=order, width=1.25, sponge=1, **kw)
+    cfg["IC_CENTER_X"] = 0.3  # off-centre so every axis sees asymmetric data
+    cfg["IC_CENTER_Y"] = -0.2
+    cfg["IC_CENTER_Z"] = 0.1
+    cfg["IC_VX_AMPLITUDE"] = 0.001
+    cfg["IC_VZ_AMPLITUDE"] = -0.0005
+    cfg["DT"] = W.cfl_dt(cfg)
+    return cfg
+
+
+def compare_state(cfg, s, o, tol):
+    r_g, v_g = s.state()
+    r_o, v_o = o.state()
+    ep = max_rel(pressure(cfg, r_g), pressure(cfg, r_o))
+    ev = max_rel(v_g, v_o)
+    assert ep <= tol and ev <= tol, (ep, ev)
+    return ep, ev
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5, 6, 7])
+def test_rhs_matches_oracle(order, solver_for, oracle_for):
+    cfg = small(order=order)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    r_g, v_g = s.rhs()
+    r_o, v_o = o.rhs()
+    assert max_rel(r_g, r_o) <= RHS_TOL
+    for a in range(3):
+        assert max_rel(v_g[a], v_o[a]) <= RHS_TOL
+
+
+@pytest.mark.parametrize("order", [2, 3, 4, 5])
+def test_steps_match_oracle(order, solver_for, oracle_for):
+    cfg = small(order=order)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 6)
+    o.run(cfg["DT"], 6)
+    compare_state(cfg, s, o, STEP_TOL)
+    assert abs(s.time - o.time) < 1e-15
+
+
+def test_config1_short_matches_oracle(solver_for, oracle_for):
+    cfg = workloads().config1(seed=0)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 10)
+    o.run(cfg["DT"], 10)
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+@pytest.mark.parametrize("periodic", [(1, 0, 0), (0, 1, 1), (1, 1, 1)])
+def test_periodic_matches_oracle(periodic, solver_for, oracle_for):
+    cfg = small(order=3, periodic=periodic)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 5)
+    o.run(cfg["DT"], 5)
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_no_diffusion_no_sponge(solver_for, oracle_for):
+    cfg = small(order=3, diffusion=False)
+    cfg["EVALUATE_SPONGE"] = 0
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 5)
+    o.run(cfg["DT"], 5)
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_linear_mass_flux(solver_for, oracle_for):
+    cfg = small(order=3)
+    cfg["B_OVER_A"] = 0.0
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 5)
+    o.run(cfg["DT"], 5)
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_multiblock_equivalent_to_single_block(solver_for, oracle_for):
+    """2x2x2 blocks with the on-device face gather == one block of the same
+    global mesh (the reference's MPI exchange makes them identical)."""
+    cfg1 = small(order=3, ne=(6, 4, 6))
+    cfg8 = dict(cfg1)
+    cfg8["NUM_ELEMENTS"] = [3, 2, 3]
+    cfg8["NUM_BLOCKS"] = [2, 2, 2]
+    s1, s8 = solver_for(cfg1), solver_for(cfg8)
+    rng = np.random.default_rng(3)
+    r = rng.standard_normal(s1.dims) * 1e-3
+    v = rng.standard_normal((3,) + s1.dims) * 1e-6
+    s1.set_state(r, v)
+    s8.set_state(r, v)
+    s1.step(cfg1["DT"], 4)
+    s8.step(cfg1["DT"], 4)
+    r1, v1 = s1.state()
+    r8, v8 = s8.state()
+    assert np.array_equal(r1, r8) and np.array_equal(v1, v8)
+    # and the multi-block IC run matches the oracle
+    o = oracle_for(cfg8)
+    s = solver_for(cfg8)
+    s.step(cfg8["DT"], 4)
+    o.run(cfg8["DT"], 4)
+    compare_state(cfg8, s, o, STEP_TOL)
+
+
+def test_tone_burst_source_matches_oracle(solver_for, oracle_for):
+    W = workloads()
+    cfg = W.scaled(W.config2(seed=0), (6, 6, 8))
+    cfg["ORDER"] = 3
+    cfg["SRC_RADIUS"] = 1.2
+    cfg["DT"] = W.cfl_dt(cfg)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    n = 40
+    s.step(cfg["DT"], n)
+    o.run(cfg["DT"], n)
+    r, _ = o.state()
+    assert np.max(np.abs(r)) > 1e-3  # the burst has entered the domain
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_set_state_clears_ic_halo(solver_for, oracle_for):
+    cfg = small(order=2)
+    s, o = solver_for(cfg), oracle_for(cfg)
+    r, v = o.state()
+    s.set_state(r, v)
+    o.set_state(r, v)
+    s.step(cfg["DT"], 3)
+    o.run(cfg["DT"], 3)
+    compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_fp32_form_within_tolerance(solver_for, oracle_for):
+    """FP32 fields/fluxes/stages with the Kahan-compensated update against the
+    FP64 oracle: relative L2 pressure error <= 1e-5."""
+    cfg = workloads().config1(seed=0)
+    cfg32 = dict(cfg)
+    cfg32["PRECISION"] = 32
+    s, o = solver_for(cfg32), oracle_for(cfg)
+    n = 50
+    s.step(cfg["DT"], n)
+    o.run(cfg["DT"], n)
+    r_g, _ = s.state()
+    r_o, _ = o.state()
+    p_g, p_o = pressure(cfg, r_g), pressure(cfg, r_o)
+    l2 = np.linalg.norm(p_g - p_o) / np.linalg.norm(p_o)
+    assert l2 <= 1e-5, l2
