@@ -88,6 +88,10 @@ def lib():
             "dg_time": (d, [vp]),
             "dg_write_snapshot": (i, [vp, cp, i, i]),
             "dg_launch_count": (C.c_longlong, [vp]),
+            "dg_hdf5_write": (i, [cp, cp, i, C.POINTER(C.c_longlong), vp, d]),
+            "dg_stream": (i, [vp, C.POINTER(vp)]),
+            "dg_profile": (i, [vp, i]),
+            "dg_kernel_stats": (i, [vp, i, C.POINTER(C.c_longlong), C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
             "dg_state_device": (i, [vp, C.POINTER(vp), C.POINTER(C.c_size_t), C.POINTER(i)]),
             "dg_last_error": (cp, []),
             "dg_write_basis_files": (i, [cp, i, i]),
@@ -238,6 +242,23 @@ class Solver:
     def launches(self) -> int:
         return lib().dg_launch_count(self.h)
 
+    @property
+    def stream(self) -> int:
+        """The handle's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        s = C.c_void_p()
+        _check(lib().dg_stream(self.h, C.byref(s)), "dg_stream")
+        return s.value or 0
+
+    def profile(self, enable: bool = True):
+        _check(lib().dg_profile(self.h, int(enable)), "dg_profile")
+
+    def kernel_stats(self, kind: int):
+        """(launches, ms, algorithmic bytes, flops) of kernel kind 0 (stage) or 1 (LDG gradient)."""
+        n, ms, b, f = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        _check(lib().dg_kernel_stats(self.h, int(kind), C.byref(n), C.byref(ms), C.byref(b), C.byref(f)),
+               "dg_kernel_stats")
+        return n.value, ms.value, b.value, f.value
+
     def write_snapshot(self, folder: str, ts: int, grid: bool = False):
         _check(lib().dg_write_snapshot(self.h, _b(folder), int(ts), int(grid)), "dg_write_snapshot")
 
@@ -257,6 +278,13 @@ def line_operators(order: int, lumped: bool = False, matrix_file=None, coeff_fil
                                    _ptr(out["stiff"]), _ptr(out["deriv"]), _ptr(out["lift0"]),
                                    _ptr(out["liftN"]), _ptr(out["zeros"])), "dg_line_operators")
     return out
+
+
+def hdf5_write(path: str, name: str, data, time: float = 0.0):
+    """One float64 dataset + "time" in the reference's HDF5 file layout."""
+    a = np.ascontiguousarray(data, dtype=np.float64)
+    dims = (C.c_longlong * a.ndim)(*a.shape)
+    _check(lib().dg_hdf5_write(_b(path), name.encode(), a.ndim, dims, _ptr(a), float(time)), "dg_hdf5_write")
 
 
 def write_basis_files(folder: str, kmax: int = 10, lumped: bool = False):

@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 LIB_CU = ["dg_solver.cu"]
 LIB_CPP = ["basis.cpp", "mesh.cpp", "params.cpp", "h5lite.cpp", "snapshot.cpp"]
-DRIVER_CPP = ["host/Basis.cpp", "host/Grid.cpp", "host/driver.cpp"]
+DRIVER_CPP = ["host/Basis.cpp", "host/Grid.cpp", "host/HDF5Functions.cpp", "host/driver.cpp"]
 
 
 def _cuda_home() -> str:
@@ -84,6 +84,16 @@ def build(verbose: bool = False, driver: bool = True) -> str:
         if r.returncode != 0:
             raise RuntimeError("driver link failed:\n%s\n%s" % (r.stdout, r.stderr))
     return LIB
+
+
+def run_peak_probe() -> str:
+    """Build and run csrc/probe/peak_probe.cu (FP64/FP32 FMA and copy throughput)."""
+    exe = os.path.join(PKG, "bin", "peak_probe")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    subprocess.check_call(["nvcc"] + ARCH + ["-O3", "-o", exe, os.path.join(CSRC, "probe", "peak_probe.cu")])
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    print(out)
+    return out
 
 
 if __name__ == "__main__":

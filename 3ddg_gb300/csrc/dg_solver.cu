@@ -92,13 +92,56 @@ OpConst<T, K> make_const(const dg_params& p, const LineOperators& op)
     return C;
 }
 
+// Algorithmic cost of one launch: every node's stage data moved once (values
+// actually needed, neighbour faces assumed served from L2) and the FP
+// operations of the formulas in dg_kernels.cuh (an FMA counts 2).
+template <typename T>
+double grad_bytes(const Solver& s, const StageIO<T>& io)
+{
+    const double nn = (double)s.gsize();
+    return (1.0 + (io.inc ? 1.0 : 0.0) + 3.0) * sizeof(T) * nn;
+}
+
+double grad_flops(const Solver& s)
+{
+    const double K = s.mesh.K;
+    return (3.0 * (2.0 * K + 5.0) + 2.0 * 6.0 / K) * (double)s.gsize();
+}
+
+template <typename T, bool INCR>
+double stage_bytes(const Solver& s, const StageIO<T>& io)
+{
+    const double nn = (double)s.gsize();
+    const double diff = s.p.eval_diff ? 3.0 : 0.0;
+    double vals;
+    if (!INCR) vals = 4.0 + diff + (io.old ? 4.0 : 0.0) + 4.0;
+    else vals = 4.0 + (io.inc ? 4.0 : 0.0) + diff + 4.0 + (io.final_stage ? 8.0 : 0.0);
+    return vals * sizeof(T) * nn;
+}
+
+double stage_flops(const Solver& s, bool has_old)
+{
+    const double K = s.mesh.K;
+    const bool diff = s.p.eval_diff, adv = s.p.eval_advect, sponge = s.p.eval_sponge;
+    double f = 6.0 + 6.0;                                  // volume fluxes
+    f += 6.0 / K * (24.0 + (diff ? 2.0 : 0.0));            // face fluxes (6K^2 face nodes per element)
+    if (diff) f += 3.0 * (2.0 * K + 6.0);                  // LDG divergence
+    if (adv) f += 3.0 * (4.0 * K + 14.0);                  // advection volume + lift
+    if (sponge) f += 8.0;
+    f += 4.0 * (3.0 + (has_old ? 2.0 : 0.0));              // RK combination
+    return f * (double)s.gsize();
+}
+
 template <typename T, int K, bool INCR>
 void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 {
     const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
+    cudaEvent_t ev = nullptr;
+    s.prof_begin(1, &ev);
     ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, C);
+    s.prof_end(1, ev, grad_bytes(s, io), grad_flops(s));
     s.launches++;
 }
 
@@ -108,10 +151,13 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
     const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
+    cudaEvent_t ev = nullptr;
+    s.prof_begin(0, &ev);
     if (s.p.eval_diff)
         stage_kernel<T, K, true, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
     else
         stage_kernel<T, K, false, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
+    s.prof_end(0, ev, stage_bytes<T, INCR>(s, io), stage_flops(s, io.old != nullptr || io.inc != nullptr));
     s.launches++;
 }
 
@@ -409,9 +455,59 @@ int Solver::init(const dg_params& prm, const char* matrix_file, const char* coef
     return DG_OK;
 }
 
+cudaEvent_t Solver::take_event()
+{
+    if (!event_pool.empty()) {
+        cudaEvent_t e = event_pool.back();
+        event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+void Solver::prof_begin(int k, cudaEvent_t* a)
+{
+    (void)k;
+    *a = nullptr;
+    if (!profiling) return;
+    *a = take_event();
+    if (*a) cudaEventRecord(*a, stream);
+}
+
+void Solver::prof_end(int k, cudaEvent_t a, double bytes, double flops)
+{
+    if (!profiling) return;
+    KernelStat& st = kstat[k];
+    st.launches++;
+    st.bytes += bytes;
+    st.flops += flops;
+    if (!a) return;
+    cudaEvent_t b = take_event();
+    if (!b) return;
+    cudaEventRecord(b, stream);
+    st.ev.emplace_back(a, b);
+}
+
+void Solver::prof_reset()
+{
+    for (KernelStat& st : kstat) {
+        for (auto& pr : st.ev) {
+            event_pool.push_back(pr.first);
+            event_pool.push_back(pr.second);
+        }
+        st.ev.clear();
+        st.launches = 0;
+        st.bytes = st.flops = 0.0;
+    }
+}
+
 Solver::~Solver()
 {
     if (stream) cudaStreamSynchronize(stream);
+    prof_reset();
+    for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
     for (void* b : buf)
         if (b) cudaFree(b);
     if (qbuf) cudaFree(qbuf);
@@ -521,6 +617,41 @@ int dg_get_grid(dg_handle* h, double* coords, double* sigma)
 double dg_time(const dg_handle* h) { return h ? h->s.t : 0.0; }
 
 long long dg_launch_count(const dg_handle* h) { return h ? h->s.launches : 0; }
+
+int dg_stream(dg_handle* h, void** stream)
+{
+    if (!h || !stream) return fail(DG_ERR_INVALID, "dg_stream: null argument");
+    *stream = (void*)h->s.stream;
+    return DG_OK;
+}
+
+int dg_profile(dg_handle* h, int enable)
+{
+    if (!h) return fail(DG_ERR_INVALID, "dg_profile: null handle");
+    cudaError_t e = cudaStreamSynchronize(h->s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    if (enable) h->s.prof_reset();
+    h->s.profiling = enable != 0;
+    return DG_OK;
+}
+
+int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double* bytes, double* flops)
+{
+    if (!h || k < 0 || k > 1) return fail(DG_ERR_INVALID, "dg_kernel_stats: bad argument");
+    cudaError_t e = cudaStreamSynchronize(h->s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    const Solver::KernelStat& st = h->s.kstat[k];
+    double total = 0.0;
+    for (const auto& pr : st.ev) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess) total += t;
+    }
+    if (launches) *launches = st.launches;
+    if (ms) *ms = total;
+    if (bytes) *bytes = st.bytes;
+    if (flops) *flops = st.flops;
+    return DG_OK;
+}
 
 int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem)
 {

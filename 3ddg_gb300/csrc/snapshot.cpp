@@ -39,18 +39,37 @@ void block_slice(const dg::MeshHost& m, const double* g, int nf, int b, std::vec
 
 }  // namespace
 
+extern "C" int dg_hdf5_write(const char* path, const char* name, int ndim, const long long* dims,
+                             const double* data, double time)
+{
+    if (!path || !name || !dims || !data || ndim < 1 || ndim > 8)
+        return dg::fail(DG_ERR_INVALID, "dg_hdf5_write: bad argument");
+    std::vector<uint64_t> d;
+    for (int i = 0; i < ndim; i++) {
+        if (dims[i] < 1) return dg::fail(DG_ERR_INVALID, "dg_hdf5_write: dimensions must be >= 1");
+        d.push_back((uint64_t)dims[i]);
+    }
+    if (std::string(name) == "time") return dg::fail(DG_ERR_INVALID, "dg_hdf5_write: name 'time' is reserved");
+    if (dg::h5_write(path, {{name, d, data}, {"time", {1}, &time}}))
+        return dg::fail(-1, "HDF5 FileIException error");
+    return DG_OK;
+}
+
 extern "C" int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int grid)
 {
-    if (!h || !folder) return dg::fail(DG_ERR_INVALID, "dg_write_snapshot: null argument");
+    if (!h || !folder || grid < 0 || grid > 2) return dg::fail(DG_ERR_INVALID, "dg_write_snapshot: bad argument");
     dg::Solver& s = h->s;
     const dg::MeshHost& m = s.mesh;
     const std::string dir(folder);
     mkdir(dir.c_str(), S_IRWXU | S_IRWXG | S_IROTH | S_IXOTH);
     mkdir((dir + "/raw").c_str(), S_IRWXU | S_IRWXG | S_IROTH | S_IXOTH);
     const size_t gs = s.gsize();
-    std::vector<double> state(4 * gs);
-    int rc = s.pack_out(s.state_ptr(), state.data(), state.data() + gs);
-    if (rc) return rc;
+    std::vector<double> state;
+    if (grid != 2) {
+        state.resize(4 * gs);
+        int rc = s.pack_out(s.state_ptr(), state.data(), state.data() + gs);
+        if (rc) return rc;
+    }
     std::vector<double> coords, sigma;
     if (grid) {
         coords.resize(3 * gs);
@@ -62,12 +81,14 @@ extern "C" int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int g
     const double tm = s.t;
     std::vector<double> a, v, c, cst;
     for (int b = 0; b < nblocks; b++) {
-        block_slice(m, state.data(), 1, b, a);
-        block_slice(m, state.data() + gs, 3, b, v);
-        if (dg::h5_write(fname(dir, "dRho", b, ts), {{"rho", {Xb, Yb, Zb}, a.data()}, {"time", {1}, &tm}}))
-            return dg::fail(-1, "HDF5 FileIException error");
-        if (dg::h5_write(fname(dir, "vel", b, ts), {{"velocity", {3, Xb, Yb, Zb}, v.data()}, {"time", {1}, &tm}}))
-            return dg::fail(-1, "HDF5 FileIException error");
+        if (grid != 2) {
+            block_slice(m, state.data(), 1, b, a);
+            block_slice(m, state.data() + gs, 3, b, v);
+            if (dg::h5_write(fname(dir, "dRho", b, ts), {{"rho", {Xb, Yb, Zb}, a.data()}, {"time", {1}, &tm}}))
+                return dg::fail(-1, "HDF5 FileIException error");
+            if (dg::h5_write(fname(dir, "vel", b, ts), {{"velocity", {3, Xb, Yb, Zb}, v.data()}, {"time", {1}, &tm}}))
+                return dg::fail(-1, "HDF5 FileIException error");
+        }
         if (grid) {
             block_slice(m, coords.data(), 3, b, c);
             if (dg::h5_write(fname(dir, "coords", b, ts), {{"coords", {3, Xb, Yb, Zb}, c.data()}, {"time", {1}, &tm}}))

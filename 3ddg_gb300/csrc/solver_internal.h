@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "basis.h"
 #include "dg3d.h"
@@ -38,6 +40,20 @@ struct Solver {
     double t = 0.0;
     long long steps_done = 0;
     long long launches = 0;
+
+    // Optional per-launch event timing (dg_profile / dg_kernel_stats).
+    struct KernelStat {
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+        long long launches = 0;
+        double bytes = 0.0, flops = 0.0;
+    };
+    bool profiling = false;
+    KernelStat kstat[2];
+    std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t take_event();
+    void prof_begin(int k, cudaEvent_t* a);
+    void prof_end(int k, cudaEvent_t a, double bytes, double flops);
+    void prof_reset();
 
     bool fp64() const { return p.precision == DG_PRECISION_FP64; }
     size_t gsize() const { return (size_t)mesh.n_elem * mesh.K * mesh.K * mesh.K; }

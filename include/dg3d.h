@@ -134,14 +134,39 @@ double dg_time(const dg_handle* h);
 /* Write the reference's snapshot files for time step ts into folder/raw/:
  * dRho_<b>_<ts>.h5 ("rho" [X][Y][Z] f64 + "time") and vel_<b>_<ts>.h5
  * ("velocity" [3][X][Y][Z] + "time"), one file pair per block b like one MPI
- * rank of the reference (cppsrc/HDF5Functions.cpp:145-247); with grid != 0
- * also coords/ba/diff/rho0/c0 (cppsrc/HDF5Functions.cpp:34-142).  The state is
- * copied back from the device only here.  Returns 0, or the reference's codes
- * -1..-4 for file/dataset failures. */
+ * rank of the reference (cppsrc/HDF5Functions.cpp:145-247).  grid = 1 adds,
+ * and grid = 2 writes only, the coords/ba/diff/rho0/c0 files of
+ * dumpGridToHDF5File (cppsrc/HDF5Functions.cpp:34-142).  The state is copied
+ * back from the device only here.  Returns 0, or the reference's codes -1..-4
+ * for file/dataset failures. */
 int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int grid);
+
+/* Write one HDF5 file holding the float64 dataset ``name`` of rank ndim
+ * (dims[0..ndim-1], row-major data) and the one-element float64 dataset
+ * "time"; replaces hdf5outputScalar / hdf5outputVector
+ * (cppsrc/HDF5Functions.cpp:249-397, whose vector form writes [3][X][Y][Z]).
+ * Host only.  Returns 0, or -1 when the file cannot be written. */
+int dg_hdf5_write(const char* path, const char* name, int ndim, const long long* dims,
+                  const double* data, double time);
 
 /* Number of kernel launches issued by this handle since creation (profiling). */
 long long dg_launch_count(const dg_handle* h);
+
+/* The cudaStream_t the handle issues all its work on (as void*), so callers
+ * can order their own work against it or time it with CUDA events. */
+int dg_stream(dg_handle* h, void** stream);
+
+/* Per-kernel statistics for profiling (no reference counterpart; the
+ * reference only had gprof).  dg_profile(h, 1) clears the counters and starts
+ * bracketing every stage / LDG-gradient kernel launch with CUDA events on the
+ * handle's stream; dg_profile(h, 0) stops.  dg_kernel_stats waits for the
+ * stream and returns, per kernel kind k (0 = stage kernel, 1 = LDG gradient),
+ * the number of launches, their summed event time in ms, and their summed
+ * algorithmic DRAM bytes and FP flops (the data each launch must move once and
+ * the arithmetic it must do, as counted in the design doc). */
+int dg_profile(dg_handle* h, int enable);
+int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double* bytes,
+                    double* flops);
 
 /* Device pointers of the current state fields (FP64 or FP32 per precision),
  * element-major: field f, element e, node n at base[f] + e*node_stride + n,
