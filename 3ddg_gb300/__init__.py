@@ -84,6 +84,7 @@ def lib():
             "dg_get_state": (i, [vp, vp, vp]),
             "dg_set_state": (i, [vp, vp, vp]),
             "dg_eval_rhs": (i, [vp, vp, vp]),
+            "dg_eval_rhs_noalloc": (i, [C.POINTER(DgParams), vp, vp, vp, vp, vp, vp, i, vp]),
             "dg_get_grid": (i, [vp, vp, vp]),
             "dg_time": (d, [vp]),
             "dg_write_snapshot": (i, [vp, cp, i, i]),

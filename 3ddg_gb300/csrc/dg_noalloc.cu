@@ -1,0 +1,233 @@
+// dg_eval_rhs_noalloc: the right-hand-side evaluation of dg_eval_rhs for
+// callers that cannot allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc is not allowed or not wanted
+// at call time — a host that owns all device memory through its own pool or
+// a fixed arena (simulation frameworks, embedded real-time loops), or code that
+// must not add allocations to a process whose memory is budgeted.  Such a
+// caller cannot create a dg_handle (dg_create allocates the state, stage and
+// gradient buffers); it already holds the state and the mesh tables in memory
+// it owns and only needs R = L(u) computed.
+//
+// The one scratch this computation needs, the LDG gradient Q (3 fields per
+// node), lives in a file-scope static device array instead of an allocation:
+// every GPU that loads this library holds it (27 MiB) until the process exits.
+// Its device address is looked up once per device with cudaGetSymbolAddress
+// (host code cannot use the array's name as a device address).  Every call
+// shares the array and it keeps the last call's contents: the gradient part is
+// fully rewritten by each call before it is read, the boundary-flag part is
+// cleared by each call, and calls whose work overlaps on the same GPU (for
+// example calls issued to two streams with no ordering between them) race on
+// it.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "dg3d.h"
+#include "dg_kernels.cuh"
+#include "solver_internal.h"
+
+namespace {
+
+constexpr size_t kMaxSlots = DG_NOALLOC_MAX_NODES;    // n_elem * NP, padded node slots
+constexpr size_t kMaxElems = DG_NOALLOC_MAX_ELEMENTS;
+constexpr size_t kQBytes = 3 * kMaxSlots * sizeof(double);
+constexpr size_t kFlagBytes = 6 * kMaxElems * sizeof(int);
+
+// LDG gradient (3 x kMaxSlots doubles) followed by the boundary-source flags
+// (6 x kMaxElems ints, zero: every boundary face reads a zero exterior state).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kQBytes + kFlagBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Set-up, once per device, with that device current.
+int scratch_address(void** out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: device index too large");
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return dg::fail(DG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_scratch_addr[dev] = ptr;
+    }
+    *out = g_scratch_addr[dev];
+    return DG_OK;
+}
+
+// D = M^-1 S and the lift columns M^-1 e_0, M^-1 e_N, on the stack.
+bool line_operators_stack(int K, const double* M, const double* S, double* D, double* L0, double* LN)
+{
+    double A[64], B[64 + 16];
+    const int R = K + 2;
+    for (int i = 0; i < K * K; i++) A[i] = M[i];
+    for (int i = 0; i < K; i++) {
+        for (int j = 0; j < K; j++) B[i * R + j] = S[i * K + j];
+        B[i * R + K] = i == 0 ? 1.0 : 0.0;
+        B[i * R + K + 1] = i == K - 1 ? 1.0 : 0.0;
+    }
+    for (int c = 0; c < K; c++) {
+        int piv = c;
+        for (int i = c + 1; i < K; i++)
+            if (std::fabs(A[i * K + c]) > std::fabs(A[piv * K + c])) piv = i;
+        if (A[piv * K + c] == 0.0) return false;
+        if (piv != c) {
+            for (int j = 0; j < K; j++) std::swap(A[c * K + j], A[piv * K + j]);
+            for (int r = 0; r < R; r++) std::swap(B[c * R + r], B[piv * R + r]);
+        }
+        for (int i = c + 1; i < K; i++) {
+            const double m = A[i * K + c] / A[c * K + c];
+            for (int j = c; j < K; j++) A[i * K + j] -= m * A[c * K + j];
+            for (int r = 0; r < R; r++) B[i * R + r] -= m * B[c * R + r];
+        }
+    }
+    for (int r = 0; r < R; r++)
+        for (int i = K - 1; i >= 0; i--) {
+            double v = B[i * R + r];
+            for (int j = i + 1; j < K; j++) v -= A[i * K + j] * B[j * R + r];
+            B[i * R + r] = v / A[i * K + i];
+        }
+    for (int i = 0; i < K; i++) {
+        for (int j = 0; j < K; j++) D[i * K + j] = B[i * R + j];
+        L0[i] = B[i * R + K];
+        LN[i] = B[i * R + K + 1];
+    }
+    return true;
+}
+
+template <int K>
+dg::OpConst<double, K> op_const(const dg_params& p, const double* M, const double* D, const double* L0,
+                                const double* LN)
+{
+    dg::OpConst<double, K> C;
+    std::memset(&C, 0, sizeof C);
+    for (int i = 0; i < K; i++) {
+        for (int j = 0; j < K; j++) C.D[i][j] = D[i * K + j];
+        C.L0[i] = L0[i];
+        C.LN[i] = LN[i];
+    }
+    const double r0 = p.rho0, c0 = p.c0;
+    for (int a = 0; a < 3; a++) {
+        const double w = p.elem_width[a];
+        C.inv_w[a] = 1.0 / w;
+        C.s_mom[a] = -1.0 / (r0 * w);
+        C.s_mass[a] = -r0 / w;
+        C.s_diff[a] = -p.diff_const / w;
+    }
+    // face-flux coefficients as the reference forms them (cppsrc/Element.cpp:542-595)
+    const double z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
+    const double cL0[4] = {z1 * r2 / (z1 + z2), z2 * r1 / (z1 + z2), z1 * z2 / r2 / (z1 + z2),
+                           -1.0 * z1 * z2 / r1 / (z1 + z2)};
+    const double cL1[4] = {z2 / r2 / (z1 + z2), z1 / r1 / (z1 + z2), r2 / (z1 + z2), -1.0 * r1 / (z1 + z2)};
+    const double cR0[4] = {z2 * r1 / (z1 + z2), z1 * r2 / (z1 + z2), z1 * z2 / r1 / (z1 + z2),
+                           -1.0 * z1 * z2 / r2 / (z1 + z2)};
+    const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
+    for (int i = 0; i < 4; i++) {
+        C.cL0[i] = cL0[i];
+        C.cL1[i] = cL1[i];
+        C.cR0[i] = cR0[i];
+        C.cR1[i] = cR1[i];
+    }
+    C.ba = p.b_over_a;
+    C.inv_r0 = 1.0 / r0;
+    C.c2_r0 = c0 * c0 / r0;
+    C.r0 = r0;
+    C.inv_c2 = 1.0 / (c0 * c0);
+    C.inv_z = 1.0 / (r0 * c0);
+    C.linear_mass = p.b_over_a == 0.0 ? 1 : 0;
+    bool diag = true;
+    for (int i = 0; i < K; i++)
+        for (int j = 0; j < K; j++)
+            if (i != j && M[i * K + j] != 0.0) diag = false;
+    C.dense_lift = diag ? 0 : 1;
+    return C;
+}
+
+template <int K>
+void launch(const dg_params& p, const dg::OpConst<double, K>& C, const dg::StageIO<double>& io,
+            const dg::MeshDev<double>& md, cudaStream_t st)
+{
+    dim3 block(dg::npt_of(K), dg::epb_of(K));
+    dim3 grid((md.n_elem + dg::epb_of(K) - 1) / dg::epb_of(K));
+    if (p.eval_diff) {
+        dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, C);
+        dg::stage_kernel<double, K, true, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
+    } else {
+        dg::stage_kernel<double, K, false, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
+    }
+}
+
+}  // namespace
+
+extern "C" int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const double* stiff,
+                                   const double* d_state, const int* d_nbr, const double* d_sigma,
+                                   double* d_rhs, int n_elem, void* stream)
+{
+    if (!p || !mass || !stiff || !d_state || !d_nbr || !d_rhs || (p->eval_sponge && !d_sigma))
+        return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: null argument");
+    if (p->precision != DG_PRECISION_FP64)
+        return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: FP64 only");
+    if (p->order < 1 || p->order > 7) return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: ORDER must be in 1..7");
+    if (!(p->rho0 > 0.0) || !(p->c0 > 0.0)) return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: bad medium");
+    const int K = p->order + 1;
+    const long long np = (K * K * K + 7) / 8 * 8;
+    if (n_elem < 1) return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: n_elem must be >= 1");
+    if ((unsigned long long)n_elem > kMaxElems || (unsigned long long)(n_elem * np) > kMaxSlots)
+        return dg::fail(DG_ERR_INVALID,
+                        "dg_eval_rhs_noalloc: problem too large for the static scratch: n_elem = " +
+                            std::to_string(n_elem) + " with " + std::to_string(np) +
+                            " node slots per element exceeds the maximum of " + std::to_string(kMaxElems) +
+                            " elements and " + std::to_string(kMaxSlots) + " node slots");
+    double D[64], L0[8], LN[8];
+    if (!line_operators_stack(K, mass, stiff, D, L0, LN))
+        return dg::fail(DG_ERR_INVALID, "dg_eval_rhs_noalloc: mass matrix is singular");
+    void* scratch = nullptr;
+    int rc = scratch_address(&scratch);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    double* q = (double*)scratch;
+    int* flags = (int*)((unsigned char*)scratch + kQBytes);
+    cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)6 * n_elem * sizeof(int), st);
+    if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+
+    dg::StageIO<double> io;
+    std::memset(&io, 0, sizeof io);
+    io.src = d_state;
+    io.dst = d_rhs;
+    io.q = q;
+    io.q_out = q;
+    io.fs = (size_t)n_elem * np;
+    io.np = (int)np;
+    io.ca = 1.0;
+    io.cb = 0.0;
+    dg::MeshDev<double> md;
+    md.nbr = d_nbr;
+    md.sigma = d_sigma;
+    md.bnd_ic = nullptr;
+    md.bnd_ap = nullptr;
+    md.bnd_src = flags;
+    md.n_elem = n_elem;
+    md.ic_live = 0;
+    md.src_p = 0.0;
+    switch (K) {
+    case 2: launch<2>(*p, op_const<2>(*p, mass, D, L0, LN), io, md, st); break;
+    case 3: launch<3>(*p, op_const<3>(*p, mass, D, L0, LN), io, md, st); break;
+    case 4: launch<4>(*p, op_const<4>(*p, mass, D, L0, LN), io, md, st); break;
+    case 5: launch<5>(*p, op_const<5>(*p, mass, D, L0, LN), io, md, st); break;
+    case 6: launch<6>(*p, op_const<6>(*p, mass, D, L0, LN), io, md, st); break;
+    case 7: launch<7>(*p, op_const<7>(*p, mass, D, L0, LN), io, md, st); break;
+    case 8: launch<8>(*p, op_const<8>(*p, mass, D, L0, LN), io, md, st); break;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return DG_OK;
+}

@@ -124,6 +124,33 @@ int dg_set_state(dg_handle* h, const double* drho, const double* vel);
  * 655-704).  The state and time are unchanged.  Synchronous. */
 int dg_eval_rhs(dg_handle* h, double* drho, double* vel);
 
+/* Size limits of dg_eval_rhs_noalloc's static scratch. */
+#define DG_NOALLOC_MAX_NODES 1048576    /* n_elem * NP node slots, NP = (N+1)^3 rounded up to 8 */
+#define DG_NOALLOC_MAX_ELEMENTS 131072
+
+/* The evaluation of dg_eval_rhs for callers that cannot allocate device
+ * memory (no counterpart in the reference; it exists for hosts that own all
+ * device memory through their own pool or arena, or must not allocate at call
+ * time, and therefore cannot create a dg_handle).  The caller passes device
+ * buffers it owns: d_state (4 FP64 fields drho, u_x, u_y, u_z, element-major:
+ * field f, element e, node n at f*n_elem*NP + e*NP + n, node n = (i*K+j)*K+k),
+ * d_nbr (n_elem x 6 face table in the order -X +X -Y +Y -Z +Z: a neighbour
+ * element index, or -1 - slot with slot < 6*n_elem for a boundary face, whose
+ * exterior state is zero), d_sigma (n_elem sponge sigmas; may be NULL when
+ * eval_sponge is 0) and d_rhs (output, same layout as d_state); host mass and
+ * stiff are the (N+1)^2 unit-interval matrices of matrices.txt.  FP64 only,
+ * order 1..7, at most DG_NOALLOC_MAX_ELEMENTS elements and
+ * DG_NOALLOC_MAX_NODES node slots (larger problems are rejected with
+ * DG_ERR_INVALID).  Calls no cudaMalloc/cudaFree or other allocating routine:
+ * the LDG-gradient scratch is a 27 MiB static device array that every GPU
+ * loading this library holds until exit.  The first call on a device looks up
+ * that array's address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  Calls share the scratch: calls whose work overlaps on one GPU race.
+ * Asynchronous on ``stream`` (a cudaStream_t, NULL = the default stream). */
+int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const double* stiff,
+                        const double* d_state, const int* d_nbr, const double* d_sigma,
+                        double* d_rhs, int n_elem, void* stream);
+
 /* Node coordinates [3][X][Y][Z] and per-node sponge sigma [X][Y][Z] (either
  * may be NULL); the data of dumpGridToHDF5File (cppsrc/HDF5Functions.cpp:34-142). */
 int dg_get_grid(dg_handle* h, double* coords, double* sigma);
