@@ -1,8 +1,9 @@
 // sm_103a kernels for one stage of the DG right-hand side and its RK update.
 //
 // Two launches per RK stage (one without diffusion):
-//   ldg_gradient_kernel  Q_a = d(drho)/dx_a by LDG with the central flux
-//                        (Element::OperateQFromDRho, cppsrc/Element.cpp:623-690)
+//   ldg_gradient_kernel  G_a = -D_c d(drho)/dx_a by LDG with the central flux
+//                        (Element::OperateQFromDRho, cppsrc/Element.cpp:623-690;
+//                        stored pre-multiplied by -D_c, the diffusive flux)
 //   stage_kernel         volume + face terms of the advection operator
 //                        (Element::OperateUFromV, cppsrc/Element.cpp:475-620),
 //                        LDG divergence (Element::OperateDRhoFromQ, :691-758),
@@ -13,9 +14,19 @@
 // Mapping: one thread per node, one warp-aligned slice of NPT threads per
 // element, EPB elements per CTA.  Each element stages its volume fluxes and
 // its face fluxes in shared memory; the line sums along each axis read shared
-// memory with D = M^-1 S held in registers.  The reference's per-line QR solve
-// of (M q w) x = S q f - F becomes x = (1/w) D f - (1/(q w)) (M^-1 e_0 F_0 +
-// M^-1 e_N F_N): D and the lift columns are computed once on the host in FP64.
+// memory with the operator rows held in registers.  The reference's per-line
+// QR solve of (M q w) x = S q f - F becomes
+//     x = (1/w) D f - (1/(q w)) (M^-1 e_0 F_0 + M^-1 e_N F_N),  D = M^-1 S,
+// with D and the lift columns computed once on the host in FP64.
+//
+// The FP64 path is bound by the FP64 pipe, so every constant factor is folded
+// on the host into the per-launch operator (OpConst): the RK stage weight ca,
+// 1/w_a and the equations' lift scales go into per-axis copies of D and into
+// the face-flux coefficients, the gradient carries -D_c so that the LDG
+// divergence and the mass-flux divergence share one line sum, and the sponge
+// folds into the RK combination.  Per node and stage each axis then costs
+// 2 (K + 2) FMAs for the volume and lift terms.
+//
 // Neighbour face values are read straight from the neighbour element (same
 // block or another block of the same HBM pool) through the face table, which
 // replaces the halo ring and Grid::communicate.
@@ -29,21 +40,23 @@ namespace dg {
 __host__ __device__ constexpr int npt_of(int K) { return (K * K * K + 31) / 32 * 32; }
 __host__ __device__ constexpr int epb_of(int K) { return K <= 3 ? 4 : (K == 4 ? 2 : 1); }
 
-// Per-problem operator constants, passed by value (kernel parameter space).
+// Per-launch operator constants, passed by value (kernel parameter space).
+//   stage kernel:    D[a] = ca D / w_a;   cM, cA: face coefficients of the
+//                    momentum / mass equations times ca * (lift scale);
+//                    cQ[a] = (+0.5, -0.5) ca / w_a (central flux of G).
+//   gradient kernel: D[a] = D_c D / w_a;  cQ[a] = (+0.5, -0.5) D_c / w_a.
+// Face coefficients act on (f_mom other, f_mom self, f_mass other, f_mass self).
 template <typename T, int K>
 struct OpConst {
-    T D[K][K];             // D = M^-1 S on the unit interval
+    T D[3][K][K];
     T L0[K], LN[K];        // lift columns M^-1 e_0, M^-1 e_N
-    T inv_w[3];            // 1 / w_a
-    T s_mom[3];            // -1 / (rho0 w_a): lift scale of the momentum equation
-    T s_mass[3];           // -rho0 / w_a:     lift scale of the mass equation
-    T s_diff[3];           // -D / w_a:        scale of the LDG divergence
-    T cL0[4], cL1[4];      // left-face flux coefficients, modes 0 and 1
-    T cR0[4], cR1[4];      // right-face flux coefficients, modes 0 and 1
-    T ba, inv_r0, c2_r0, r0;  // momentum / mass flux constants
+    T cM[3][2][4];
+    T cA[3][2][4];
+    T cQ[3][2];
+    T k1, k2;              // f_mom(rho) = rho (k1 + k2 rho) = c^2/rho0 (rho + B/A rho^2 / (2 rho0))
+    T r0;                  // f_mass(u, rho) = u (rho + rho0), or u rho0 when B/A = 0
     T inv_c2, inv_z;       // source exterior state: drho = p / c^2, u = p / (rho0 c)
-    int linear_mass;       // B/A == 0 selects u*rho0 (cppsrc/kernelFuncs.cpp:25)
-    int dense_lift;        // 0 when M is diagonal (lift touches end nodes only)
+    int linear_mass;
 };
 
 // Mesh arrays on the device (see mesh.h).
@@ -59,11 +72,16 @@ struct MeshDev {
     T src_p;               // source pressure at this stage's time
 };
 
-// Stage input/output.  PLAIN (FP64 method): the stage input is ``src``,
-//   dst = ca * R + cb * src (+ cc * old).
-// INCR (FP32 form): the stage input is u + d (d = ``inc``, absent in stage 1),
-//   d_out = ca * R + cb * d + eps * u; the final stage adds d_out to u with a
-//   Kahan-compensated sum into ``dst`` (the other u buffer) and ``comp``.
+// Stage input/output.  R' = ca R_ops is what the folded operator produces
+// (R_ops: advection + diffusion, without the sponge).
+//   PLAIN (FP64 method), stage input s = ``src``:
+//       dst = R' + s (cb - ca sigma) + cc old         (= ca R + cb s + cc old)
+//   INCR (FP32 form), stage input s = u + d (u = ``src``, d = ``inc``, absent
+//   in stage 1):
+//       d_out = R' + d (cb - ca sigma) + u (eps - ca sigma)
+//                                                     (= ca R + cb d + eps u)
+//       and in the final stage u <- u + d_out with a Kahan-compensated sum
+//       into ``dst`` (the other u buffer) and ``comp``.
 template <typename T>
 struct StageIO {
     const T* src;
@@ -71,7 +89,7 @@ struct StageIO {
     const T* old;
     T* dst;
     T* comp;
-    const T* q;            // LDG gradient, 3 fields
+    const T* q;            // LDG gradient (times -D_c), 3 fields
     T* q_out;              // gradient kernel output
     size_t fs;             // field stride (n_elem * NP)
     int np;                // nodes per element in memory
@@ -80,14 +98,9 @@ struct StageIO {
 };
 
 template <typename T>
-__device__ __forceinline__ T momentum_flux(T d, const T ba, const T inv_r0, const T c2_r0)
+__device__ __forceinline__ T momentum_flux(T d, const T k1, const T k2)
 {
-    // cppsrc/kernelFuncs.cpp:19-20: (d + d*d*B/A*0.5*(1/rho0)) * (c*c/rho0)
-    T t = d * d;
-    t = t * ba;
-    t = t * T(0.5);
-    t = t * inv_r0;
-    return (d + t) * c2_r0;
+    return d * (k1 + k2 * d);
 }
 
 template <typename T>
@@ -99,10 +112,10 @@ __device__ __forceinline__ T mass_flux(T u, T d, const T r0, int linear)
 
 template <typename T, int K>
 struct StageSmem {
-    T fm[npt_of(K)];
-    T fa[3][npt_of(K)];
-    T qa[3][npt_of(K)];
-    T fl[3][2][3][K * K];  // [axis][side][mom, mass, diff][face node]
+    T fm[npt_of(K)];       // momentum flux f_mom
+    T fh[3][npt_of(K)];    // f_mass along axis a plus the LDG gradient along a
+    T gm[3][2][K * K];     // momentum face terms [axis][side][face node]
+    T gr[3][2][K * K];     // density face terms (mass + diffusion)
 };
 
 template <typename T, int K>
@@ -145,8 +158,9 @@ __device__ __forceinline__ int axis_stride(int a)
 }
 
 // ---------------------------------------------------------------------------
-// LDG gradient: Q_a = -(1/w_a) (D drho + M^-1 e_0 F_0 + M^-1 e_N F_N) with the
-// central flux F_0 = (drho_o[N] + drho_s[0]) / 2, F_N = -(drho_s[N] + drho_o[0]) / 2.
+// LDG gradient, stored as G_a = -D_c Q_a = (D_c / w_a)(D drho + M^-1 e_0 F_0 +
+// M^-1 e_N F_N) with the central flux F_0 = (drho_o[N] + drho_s[0]) / 2,
+// F_N = -(drho_s[N] + drho_o[0]) / 2.
 // ---------------------------------------------------------------------------
 template <typename T, int K, bool INCR>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
@@ -176,7 +190,7 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C)
             } else {
                 exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
             }
-            S.fl[a][side][fi] = side == 0 ? T(0.5) * (ro + rho) : T(-0.5) * (rho + ro);
+            S.fl[a][side][fi] = C.cQ[a][side] * (ro + rho);
         }
     }
     __syncthreads();
@@ -187,13 +201,11 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C)
         const int ia = c[a];
         const int base = n - ia * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T s = T(0);
+        T s = C.L0[ia] * S.fl[a][0][fi];
+        s += C.LN[ia] * S.fl[a][1][fi];
 #pragma unroll
-        for (int j = 0; j < K; j++) s += C.D[ia][j] * S.r[base + j * st];
-        T lf;
-        if (C.dense_lift) lf = C.L0[ia] * S.fl[a][0][fi] + C.LN[ia] * S.fl[a][1][fi];
-        else lf = (ia == 0 ? C.L0[ia] * S.fl[a][0][fi] : T(0)) + (ia == K - 1 ? C.LN[ia] * S.fl[a][1][fi] : T(0));
-        io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = T(-1) * (C.inv_w[a] * (s + lf));
+        for (int j = 0; j < K; j++) s += C.D[a][ia][j] * S.r[base + j * st];
+        io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
     }
 }
 
@@ -222,19 +234,19 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C, int do_adv, int do_sp
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
     }
-    const T fmom = momentum_flux(rho, C.ba, C.inv_r0, C.c2_r0);
-    T fmass[3];
+    T fmom = T(0), fmass[3] = {T(0), T(0), T(0)};
+    if (do_adv) {
+        fmom = momentum_flux(rho, C.k1, C.k2);
 #pragma unroll
-    for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, C.r0, C.linear_mass);
+        for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, C.r0, C.linear_mass);
+    }
     S.fm[n] = fmom;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        S.fa[a][n] = fmass[a];
-        if (DIFF) S.qa[a][n] = q[a];
-    }
+    for (int a = 0; a < 3; a++) S.fh[a][n] = DIFF ? fmass[a] + q[a] : fmass[a];
 
-    // Face fluxes: the thread owning a face node evaluates that face's numerical
-    // flux for its line (impedance upwind for advection, central for LDG).
+    // Face terms: the thread owning a face node evaluates that face's numerical
+    // flux for its line (impedance upwind for advection, central for LDG),
+    // already multiplied by its lift scale.
     if (act) {
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -252,87 +264,63 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C, int do_adv, int do_sp
             } else {
                 exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
             }
-            const T fmo = momentum_flux(ro, C.ba, C.inv_r0, C.c2_r0);
-            const T fao = mass_flux(uo, ro, C.r0, C.linear_mass);
-            if (side == 0) {
-                S.fl[a][0][0][fi] = T(-1) * (fmo * C.cL0[0] + fmom * C.cL0[1] + fao * C.cL0[2] + fmass[a] * C.cL0[3]);
-                S.fl[a][0][1][fi] = T(-1) * (fao * C.cL1[0] + fmass[a] * C.cL1[1] + fmo * C.cL1[2] + fmom * C.cL1[3]);
-                if (DIFF) S.fl[a][0][2][fi] = T(0.5) * (qo + q[a]);
-            } else {
-                S.fl[a][1][0][fi] = fmom * C.cR0[0] + fmo * C.cR0[1] + fmass[a] * C.cR0[2] + fao * C.cR0[3];
-                S.fl[a][1][1][fi] = fmass[a] * C.cR1[0] + fao * C.cR1[1] + fmom * C.cR1[2] + fmo * C.cR1[3];
-                if (DIFF) S.fl[a][1][2][fi] = T(-0.5) * (q[a] + qo);
+            T gm = T(0), gr = T(0);
+            if (do_adv) {
+                const T fmo = momentum_flux(ro, C.k1, C.k2);
+                const T fao = mass_flux(uo, ro, C.r0, C.linear_mass);
+                const T* cm = C.cM[a][side];
+                const T* cr = C.cA[a][side];
+                gm = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
+                gr = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3];
             }
+            if (DIFF) gr += C.cQ[a][side] * (qo + q[a]);
+            S.gm[a][side][fi] = gm;
+            S.gr[a][side][fi] = gr;
         }
     }
     __syncthreads();
     if (!act) return;
 
     T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
-    // LDG divergence first, as the reference accumulates it (cppsrc/Grid.cpp:674-689).
-    if (DIFF) {
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
-            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-            T s = T(0);
+    for (int a = 0; a < 3; a++) {
+        const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
+        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+        T sr = C.L0[ia] * S.gr[a][0][fi];
+        sr += C.LN[ia] * S.gr[a][1][fi];
 #pragma unroll
-            for (int j = 0; j < K; j++) s += C.D[ia][j] * S.qa[a][base + j * st];
-            T lf;
-            if (C.dense_lift) lf = C.L0[ia] * S.fl[a][0][2][fi] + C.LN[ia] * S.fl[a][1][2][fi];
-            else lf = (ia == 0 ? C.L0[ia] * S.fl[a][0][2][fi] : T(0)) + (ia == K - 1 ? C.LN[ia] * S.fl[a][1][2][fi] : T(0));
-            r_rho += C.s_diff[a] * (s + lf);
+        for (int j = 0; j < K; j++) sr += C.D[a][ia][j] * S.fh[a][base + j * st];
+        r_rho += sr;
+        if (do_adv) {
+            T sm = C.L0[ia] * S.gm[a][0][fi];
+            sm += C.LN[ia] * S.gm[a][1][fi];
+#pragma unroll
+            for (int j = 0; j < K; j++) sm += C.D[a][ia][j] * S.fm[base + j * st];
+            r_u[a] = sm;
         }
     }
-    if (do_adv) {
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
-            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-            T sm = T(0), sa = T(0);
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                sm += C.D[ia][j] * S.fm[base + j * st];
-                sa += C.D[ia][j] * S.fa[a][base + j * st];
-            }
-            T lm, la;
-            if (C.dense_lift) {
-                lm = C.L0[ia] * S.fl[a][0][0][fi] + C.LN[ia] * S.fl[a][1][0][fi];
-                la = C.L0[ia] * S.fl[a][0][1][fi] + C.LN[ia] * S.fl[a][1][1][fi];
-            } else {
-                lm = (ia == 0 ? C.L0[ia] * S.fl[a][0][0][fi] : T(0)) + (ia == K - 1 ? C.LN[ia] * S.fl[a][1][0][fi] : T(0));
-                la = (ia == 0 ? C.L0[ia] * S.fl[a][0][1][fi] : T(0)) + (ia == K - 1 ? C.LN[ia] * S.fl[a][1][1][fi] : T(0));
-            }
-            r_u[a] += C.inv_w[a] * sm + C.s_mom[a] * lm;
-            r_rho += C.inv_w[a] * sa + C.s_mass[a] * la;
-        }
-    }
-    if (do_sponge) {
-        const T sg = __ldg(m.sigma + e);
-#pragma unroll
-        for (int a = 0; a < 3; a++) r_u[a] += T(-1) * u[a] * sg;
-        r_rho += T(-1) * rho * sg;
-    }
+    const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);
 
     const T r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
     if (!INCR) {
         const T s4[4] = {rho, u[0], u[1], u[2]};
+        const T cbe = io.cb - ks;
 #pragma unroll
         for (int f = 0; f < 4; f++) {
             const size_t o = (size_t)f * io.fs + off;
-            T v = r[f] * io.ca + s4[f] * io.cb;
-            if (io.old) v = v + io.old[o] * io.cc;
+            T v = r[f] + s4[f] * cbe;
+            if (io.old) v += io.old[o] * io.cc;
             io.dst[o] = v;
         }
     } else {
+        const T cbe = io.cb - ks, ce = io.eps - ks;
 #pragma unroll
         for (int f = 0; f < 4; f++) {
             const size_t o = (size_t)f * io.fs + off;
             const T ub = __ldg(io.src + o);
-            T d = r[f] * io.ca;
-            if (io.inc) d += io.cb * __ldg(io.inc + o);
+            T d = r[f] + ub * ce;
+            if (io.inc) d += __ldg(io.inc + o) * cbe;
             if (io.final_stage) {
-                d += io.eps * ub;
                 // Kahan-compensated u <- u + d
                 const T y = d - io.comp[o];
                 const T t = ub + y;
@@ -343,6 +331,81 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C, int do_adv, int do_sp
             }
         }
     }
+}
+
+// Host-side construction of the per-launch operators from the FP64 line
+// operators (M^-1 S, lift columns) and the problem constants.
+// ``rk_ca`` is the stage weight of R (1 for a bare right-hand side).
+template <typename T, int K>
+inline OpConst<T, K> make_stage_const(double rk_ca, const double* deriv, const double* lift0, const double* liftN,
+                                      const double w[3], double rho0, double c0, double b_over_a,
+                                      double diff_const)
+{
+    OpConst<T, K> C{};
+    for (int i = 0; i < K; i++) {
+        C.L0[i] = (T)lift0[i];
+        C.LN[i] = (T)liftN[i];
+    }
+    // Face-flux coefficients as the reference forms them (cppsrc/Element.cpp:542-556
+    // left, :581-595 right); z = rho0 c0 and r = rho0 on both sides.
+    const double r0 = rho0, z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
+    const double cL0[4] = {z1 * r2 / (z1 + z2), z2 * r1 / (z1 + z2), z1 * z2 / r2 / (z1 + z2),
+                           -1.0 * z1 * z2 / r1 / (z1 + z2)};
+    const double cL1[4] = {z2 / r2 / (z1 + z2), z1 / r1 / (z1 + z2), r2 / (z1 + z2), -1.0 * r1 / (z1 + z2)};
+    const double cR0[4] = {z2 * r1 / (z1 + z2), z1 * r2 / (z1 + z2), z1 * z2 / r1 / (z1 + z2),
+                           -1.0 * z1 * z2 / r2 / (z1 + z2)};
+    const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
+    for (int a = 0; a < 3; a++) {
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) C.D[a][i][j] = (T)(rk_ca * deriv[i * K + j] / w[a]);
+        // momentum: lift scale -1/(rho0 w); left flux F_0 = -(fmo cL0[0] + fms cL0[1]
+        // + fao cL0[2] + fas cL0[3]), right F_N = fms cR0[0] + fmo cR0[1] + fas cR0[2] + fao cR0[3]
+        const double km = rk_ca * (-1.0 / (r0 * w[a]));
+        const double lm[4] = {-cL0[0], -cL0[1], -cL0[2], -cL0[3]};
+        const double rm[4] = {cR0[1], cR0[0], cR0[3], cR0[2]};
+        // mass: lift scale -rho0/w; left F_0 = -(fao cL1[0] + fas cL1[1] + fmo cL1[2] + fms cL1[3]),
+        // right F_N = fas cR1[0] + fao cR1[1] + fms cR1[2] + fmo cR1[3]
+        const double ka = rk_ca * (-r0 / w[a]);
+        const double la[4] = {-cL1[2], -cL1[3], -cL1[0], -cL1[1]};
+        const double ra[4] = {cR1[3], cR1[2], cR1[1], cR1[0]};
+        for (int i = 0; i < 4; i++) {
+            C.cM[a][0][i] = (T)(km * lm[i]);
+            C.cM[a][1][i] = (T)(km * rm[i]);
+            C.cA[a][0][i] = (T)(ka * la[i]);
+            C.cA[a][1][i] = (T)(ka * ra[i]);
+        }
+        // LDG divergence of G = -D_c Q: (1/w)(D G + lift(central flux of G))
+        C.cQ[a][0] = (T)(0.5 * rk_ca / w[a]);
+        C.cQ[a][1] = (T)(-0.5 * rk_ca / w[a]);
+    }
+    C.k1 = (T)(c0 * c0 / r0);
+    C.k2 = (T)(b_over_a * 0.5 * c0 * c0 / (r0 * r0));
+    C.r0 = (T)r0;
+    C.inv_c2 = (T)(1.0 / (c0 * c0));
+    C.inv_z = (T)(1.0 / (r0 * c0));
+    C.linear_mass = b_over_a == 0.0 ? 1 : 0;
+    (void)diff_const;
+    return C;
+}
+
+template <typename T, int K>
+inline OpConst<T, K> make_grad_const(const double* deriv, const double* lift0, const double* liftN,
+                                     const double w[3], double rho0, double c0, double diff_const)
+{
+    OpConst<T, K> C{};
+    for (int i = 0; i < K; i++) {
+        C.L0[i] = (T)lift0[i];
+        C.LN[i] = (T)liftN[i];
+    }
+    for (int a = 0; a < 3; a++) {
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) C.D[a][i][j] = (T)(diff_const * deriv[i * K + j] / w[a]);
+        C.cQ[a][0] = (T)(0.5 * diff_const / w[a]);
+        C.cQ[a][1] = (T)(-0.5 * diff_const / w[a]);
+    }
+    C.inv_c2 = (T)(1.0 / (c0 * c0));
+    C.inv_z = (T)(1.0 / (rho0 * c0));
+    return C;
 }
 
 // Element-major state  <->  node-duplicated [X][Y][Z] grid layout (the

@@ -105,61 +105,17 @@ bool line_operators_stack(int K, const double* M, const double* S, double* D, do
 }
 
 template <int K>
-dg::OpConst<double, K> op_const(const dg_params& p, const double* M, const double* D, const double* L0,
-                                const double* LN)
-{
-    dg::OpConst<double, K> C;
-    std::memset(&C, 0, sizeof C);
-    for (int i = 0; i < K; i++) {
-        for (int j = 0; j < K; j++) C.D[i][j] = D[i * K + j];
-        C.L0[i] = L0[i];
-        C.LN[i] = LN[i];
-    }
-    const double r0 = p.rho0, c0 = p.c0;
-    for (int a = 0; a < 3; a++) {
-        const double w = p.elem_width[a];
-        C.inv_w[a] = 1.0 / w;
-        C.s_mom[a] = -1.0 / (r0 * w);
-        C.s_mass[a] = -r0 / w;
-        C.s_diff[a] = -p.diff_const / w;
-    }
-    // face-flux coefficients as the reference forms them (cppsrc/Element.cpp:542-595)
-    const double z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
-    const double cL0[4] = {z1 * r2 / (z1 + z2), z2 * r1 / (z1 + z2), z1 * z2 / r2 / (z1 + z2),
-                           -1.0 * z1 * z2 / r1 / (z1 + z2)};
-    const double cL1[4] = {z2 / r2 / (z1 + z2), z1 / r1 / (z1 + z2), r2 / (z1 + z2), -1.0 * r1 / (z1 + z2)};
-    const double cR0[4] = {z2 * r1 / (z1 + z2), z1 * r2 / (z1 + z2), z1 * z2 / r1 / (z1 + z2),
-                           -1.0 * z1 * z2 / r2 / (z1 + z2)};
-    const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
-    for (int i = 0; i < 4; i++) {
-        C.cL0[i] = cL0[i];
-        C.cL1[i] = cL1[i];
-        C.cR0[i] = cR0[i];
-        C.cR1[i] = cR1[i];
-    }
-    C.ba = p.b_over_a;
-    C.inv_r0 = 1.0 / r0;
-    C.c2_r0 = c0 * c0 / r0;
-    C.r0 = r0;
-    C.inv_c2 = 1.0 / (c0 * c0);
-    C.inv_z = 1.0 / (r0 * c0);
-    C.linear_mass = p.b_over_a == 0.0 ? 1 : 0;
-    bool diag = true;
-    for (int i = 0; i < K; i++)
-        for (int j = 0; j < K; j++)
-            if (i != j && M[i * K + j] != 0.0) diag = false;
-    C.dense_lift = diag ? 0 : 1;
-    return C;
-}
-
-template <int K>
-void launch(const dg_params& p, const dg::OpConst<double, K>& C, const dg::StageIO<double>& io,
+void launch(const dg_params& p, const double* D, const double* L0, const double* LN, const dg::StageIO<double>& io,
             const dg::MeshDev<double>& md, cudaStream_t st)
 {
+    const dg::OpConst<double, K> C = dg::make_stage_const<double, K>(1.0, D, L0, LN, p.elem_width, p.rho0, p.c0,
+                                                                     p.b_over_a, p.diff_const);
     dim3 block(dg::npt_of(K), dg::epb_of(K));
     dim3 grid((md.n_elem + dg::epb_of(K) - 1) / dg::epb_of(K));
     if (p.eval_diff) {
-        dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, C);
+        const dg::OpConst<double, K> G =
+            dg::make_grad_const<double, K>(D, L0, LN, p.elem_width, p.rho0, p.c0, p.diff_const);
+        dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, G);
         dg::stage_kernel<double, K, true, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
     } else {
         dg::stage_kernel<double, K, false, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
@@ -219,13 +175,13 @@ extern "C" int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const
     md.ic_live = 0;
     md.src_p = 0.0;
     switch (K) {
-    case 2: launch<2>(*p, op_const<2>(*p, mass, D, L0, LN), io, md, st); break;
-    case 3: launch<3>(*p, op_const<3>(*p, mass, D, L0, LN), io, md, st); break;
-    case 4: launch<4>(*p, op_const<4>(*p, mass, D, L0, LN), io, md, st); break;
-    case 5: launch<5>(*p, op_const<5>(*p, mass, D, L0, LN), io, md, st); break;
-    case 6: launch<6>(*p, op_const<6>(*p, mass, D, L0, LN), io, md, st); break;
-    case 7: launch<7>(*p, op_const<7>(*p, mass, D, L0, LN), io, md, st); break;
-    case 8: launch<8>(*p, op_const<8>(*p, mass, D, L0, LN), io, md, st); break;
+    case 2: launch<2>(*p, D, L0, LN, io, md, st); break;
+    case 3: launch<3>(*p, D, L0, LN, io, md, st); break;
+    case 4: launch<4>(*p, D, L0, LN, io, md, st); break;
+    case 5: launch<5>(*p, D, L0, LN, io, md, st); break;
+    case 6: launch<6>(*p, D, L0, LN, io, md, st); break;
+    case 7: launch<7>(*p, D, L0, LN, io, md, st); break;
+    case 8: launch<8>(*p, D, L0, LN, io, md, st); break;
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));

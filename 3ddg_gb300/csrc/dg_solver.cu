@@ -44,54 +44,6 @@ double burst_pressure(const dg_params& p, double t)
 
 namespace {
 
-template <typename T, int K>
-OpConst<T, K> make_const(const dg_params& p, const LineOperators& op)
-{
-    OpConst<T, K> C;
-    std::memset(&C, 0, sizeof C);
-    for (int i = 0; i < K; i++) {
-        for (int j = 0; j < K; j++) C.D[i][j] = (T)op.deriv[i * K + j];
-        C.L0[i] = (T)op.lift0[i];
-        C.LN[i] = (T)op.liftN[i];
-    }
-    const double r0 = p.rho0, c0 = p.c0;
-    for (int a = 0; a < 3; a++) {
-        const double w = p.elem_width[a];
-        C.inv_w[a] = (T)(1.0 / w);
-        C.s_mom[a] = (T)(-1.0 / (r0 * w));
-        C.s_mass[a] = (T)(-r0 / w);
-        C.s_diff[a] = (T)(-p.diff_const / w);
-    }
-    // Face-flux coefficients exactly as cppsrc/Element.cpp:542-556 (left) and
-    // :581-595 (right) form them; z = rho0 c0 and r = rho0 on both sides.
-    const double z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
-    const double cL0[4] = {z1 * r2 / (z1 + z2), z2 * r1 / (z1 + z2), z1 * z2 / r2 / (z1 + z2),
-                           -1.0 * z1 * z2 / r1 / (z1 + z2)};
-    const double cL1[4] = {z2 / r2 / (z1 + z2), z1 / r1 / (z1 + z2), r2 / (z1 + z2), -1.0 * r1 / (z1 + z2)};
-    const double cR0[4] = {z2 * r1 / (z1 + z2), z1 * r2 / (z1 + z2), z1 * z2 / r1 / (z1 + z2),
-                           -1.0 * z1 * z2 / r2 / (z1 + z2)};
-    const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
-    for (int i = 0; i < 4; i++) {
-        C.cL0[i] = (T)cL0[i];
-        C.cL1[i] = (T)cL1[i];
-        C.cR0[i] = (T)cR0[i];
-        C.cR1[i] = (T)cR1[i];
-    }
-    C.ba = (T)p.b_over_a;
-    C.inv_r0 = (T)(1.0 / r0);
-    C.c2_r0 = (T)(c0 * c0 / r0);
-    C.r0 = (T)r0;
-    C.inv_c2 = (T)(1.0 / (c0 * c0));
-    C.inv_z = (T)(1.0 / (r0 * c0));
-    C.linear_mass = p.b_over_a == 0.0 ? 1 : 0;
-    bool diag = true;
-    for (int i = 0; i < K; i++)
-        for (int j = 0; j < K; j++)
-            if (i != j && op.mass[i * K + j] != 0.0) diag = false;
-    C.dense_lift = diag ? 0 : 1;
-    return C;
-}
-
 // Algorithmic cost of one launch: every node's stage data moved once (values
 // actually needed, neighbour faces assumed served from L2) and the FP
 // operations of the formulas in dg_kernels.cuh (an FMA counts 2).
@@ -104,8 +56,9 @@ double grad_bytes(const Solver& s, const StageIO<T>& io)
 
 double grad_flops(const Solver& s)
 {
+    // per axis K + 2 FMAs (line sum + two lift terms); face terms 2 flops
     const double K = s.mesh.K;
-    return (3.0 * (2.0 * K + 5.0) + 2.0 * 6.0 / K) * (double)s.gsize();
+    return (3.0 * 2.0 * (K + 2.0) + 6.0 / K * 2.0) * (double)s.gsize();
 }
 
 template <typename T, bool INCR>
@@ -122,20 +75,21 @@ double stage_bytes(const Solver& s, const StageIO<T>& io)
 double stage_flops(const Solver& s, bool has_old)
 {
     const double K = s.mesh.K;
-    const bool diff = s.p.eval_diff, adv = s.p.eval_advect, sponge = s.p.eval_sponge;
-    double f = 6.0 + 6.0;                                  // volume fluxes
-    f += 6.0 / K * (24.0 + (diff ? 2.0 : 0.0));            // face fluxes (6K^2 face nodes per element)
-    if (diff) f += 3.0 * (2.0 * K + 6.0);                  // LDG divergence
-    if (adv) f += 3.0 * (4.0 * K + 14.0);                  // advection volume + lift
-    if (sponge) f += 8.0;
-    f += 4.0 * (3.0 + (has_old ? 2.0 : 0.0));              // RK combination
+    const bool diff = s.p.eval_diff, adv = s.p.eval_advect;
+    double f = 0.0;
+    if (adv) f += 3.0 + 4.0;                              // f_mom (FMA + MUL), f_mass (ADD + 3 MUL)
+    if (diff) f += 3.0;                                   // f_mass + G per axis
+    f += 3.0 * 2.0 * (K + 2.0) * (adv ? 2.0 : 1.0);       // line sums + lifts (2 equations with advection)
+    f += 6.0 / K * ((adv ? 21.0 : 0.0) + (diff ? 3.0 : 0.0));  // face terms (6K^2 face nodes per element)
+    f += 4.0 * (2.0 + (has_old ? 2.0 : 0.0)) + 2.0;      // sponge-folded RK combination
     return f * (double)s.gsize();
 }
 
 template <typename T, int K, bool INCR>
 void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 {
-    const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
+    const OpConst<T, K> C = make_grad_const<T, K>(s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(),
+                                                  s.p.elem_width, s.p.rho0, s.p.c0, s.p.diff_const);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
@@ -146,9 +100,10 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 }
 
 template <typename T, int K, bool INCR>
-void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, double ca)
 {
-    const OpConst<T, K> C = make_const<T, K>(s.p, s.op);
+    const OpConst<T, K> C = make_stage_const<T, K>(ca, s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(),
+                                                   s.p.elem_width, s.p.rho0, s.p.c0, s.p.b_over_a, s.p.diff_const);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
@@ -176,16 +131,16 @@ void dispatch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 }
 
 template <typename T, bool INCR>
-void dispatch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
+void dispatch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, double ca)
 {
     switch (s.mesh.K) {
-    case 2: launch_stage<T, 2, INCR>(s, io, md); break;
-    case 3: launch_stage<T, 3, INCR>(s, io, md); break;
-    case 4: launch_stage<T, 4, INCR>(s, io, md); break;
-    case 5: launch_stage<T, 5, INCR>(s, io, md); break;
-    case 6: launch_stage<T, 6, INCR>(s, io, md); break;
-    case 7: launch_stage<T, 7, INCR>(s, io, md); break;
-    case 8: launch_stage<T, 8, INCR>(s, io, md); break;
+    case 2: launch_stage<T, 2, INCR>(s, io, md, ca); break;
+    case 3: launch_stage<T, 3, INCR>(s, io, md, ca); break;
+    case 4: launch_stage<T, 4, INCR>(s, io, md, ca); break;
+    case 5: launch_stage<T, 5, INCR>(s, io, md, ca); break;
+    case 6: launch_stage<T, 6, INCR>(s, io, md, ca); break;
+    case 7: launch_stage<T, 7, INCR>(s, io, md, ca); break;
+    case 8: launch_stage<T, 8, INCR>(s, io, md, ca); break;
     }
 }
 
@@ -262,7 +217,7 @@ int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
     md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
     md.src_p = burst_pressure(p, tst[s_idx]);
     if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
-    dispatch_stage<double, false>(*this, io, md);
+    dispatch_stage<double, false>(*this, io, md, io.ca);
     return DG_OK;
 }
 
@@ -277,6 +232,8 @@ int Solver::rk_stage_fp32(int s_idx, double dt, float* rhs_only)
     float* comp = (float*)buf[2];
     float* d1 = (float*)buf[3];
     float* d2 = (float*)buf[4];
+    const double cas[3] = {dt, dt * .25, dt * 2.0 / 3.0};
+    const double ca = rhs_only ? 1.0 : cas[s_idx];
     StageIO<float> io;
     std::memset(&io, 0, sizeof io);
     io.fs = mesh.fstride();
@@ -301,7 +258,7 @@ int Solver::rk_stage_fp32(int s_idx, double dt, float* rhs_only)
     md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
     md.src_p = (float)burst_pressure(p, tst[s_idx]);
     if (p.eval_diff) dispatch_grad<float, true>(*this, io, md);
-    dispatch_stage<float, true>(*this, io, md);
+    dispatch_stage<float, true>(*this, io, md, ca);
     return DG_OK;
 }
 
