@@ -90,11 +90,31 @@ def lib():
             "dg_write_snapshot": (i, [vp, cp, i, i]),
             "dg_launch_count": (C.c_longlong, [vp]),
             "dg_hdf5_write": (i, [cp, cp, i, C.POINTER(C.c_longlong), vp, d]),
+            "dg_probe_set": (i, [vp, i, vp]),
+            "dg_probe_get": (i, [vp, vp, vp, i, C.POINTER(i)]),
             "dg_stream": (i, [vp, C.POINTER(vp)]),
             "dg_profile": (i, [vp, i]),
             "dg_kernel_stats": (i, [vp, i, C.POINTER(C.c_longlong), C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
             "dg_state_device": (i, [vp, C.POINTER(vp), C.POINTER(C.c_size_t), C.POINTER(i)]),
             "dg_last_error": (cp, []),
+            "dg_batch_create": (i, [i, C.POINTER(DgParams), C.POINTER(d), C.POINTER(i), cp, cp, C.POINTER(vp)]),
+            "dg_batch_destroy": (i, [vp]),
+            "dg_batch_step": (i, [vp, i]),
+            "dg_batch_synchronize": (i, [vp]),
+            "dg_batch_get_state": (i, [vp, i, vp, vp]),
+            "dg_batch_info": (i, [vp, i, C.POINTER(i), C.POINTER(C.c_longlong), C.POINTER(d)]),
+            "dg_batch_total_nodes": (C.c_longlong, [vp]),
+            "dg_batch_autotune": (i, [vp, i, cp, C.c_size_t]),
+            "dg_batch_stream": (i, [vp, C.POINTER(vp)]),
+            "dg_batch_launch_count": (C.c_longlong, [vp]),
+            "dg_serve_create": (i, [C.c_size_t, i, C.POINTER(vp)]),
+            "dg_serve_destroy": (i, [vp]),
+            "dg_serve_clock": (d, [vp]),
+            "dg_serve_submit": (i, [vp, C.POINTER(DgParams), d, i, d, C.POINTER(C.c_longlong)]),
+            "dg_serve_tick": (i, [vp, C.POINTER(i)]),
+            "dg_serve_run": (i, [vp, d]),
+            "dg_serve_result": (i, [vp, C.c_longlong, C.POINTER(d), C.POINTER(d), C.POINTER(d), vp, vp]),
+            "dg_serve_stats": (i, [vp, C.POINTER(i), C.POINTER(d), C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
             "dg_write_basis_files": (i, [cp, i, i]),
             "dg_line_operators": (i, [i, i, cp, cp, vp, vp, vp, vp, vp, vp]),
         }
@@ -243,6 +263,21 @@ class Solver:
     def launches(self) -> int:
         return lib().dg_launch_count(self.h)
 
+    def probe_set(self, points):
+        """Record the pressure at the nodes nearest to ``points`` (n x 3) after every step."""
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        self._n_probe = len(pts)
+        _check(lib().dg_probe_set(self.h, len(pts), _ptr(pts)), "dg_probe_set")
+
+    def probe_get(self):
+        """(t [steps], p [steps, n]) recorded since probe_set."""
+        ns = C.c_int()
+        _check(lib().dg_probe_get(self.h, None, None, 0, C.byref(ns)), "dg_probe_get")
+        t = np.empty(ns.value)
+        p = np.empty((ns.value, self._n_probe))
+        _check(lib().dg_probe_get(self.h, _ptr(t), _ptr(p), ns.value, C.byref(ns)), "dg_probe_get")
+        return t, p
+
     @property
     def stream(self) -> int:
         """The handle's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
@@ -269,6 +304,157 @@ class Solver:
         ne = C.c_int()
         _check(lib().dg_state_device(self.h, base, C.byref(ns), C.byref(ne)), "dg_state_device")
         return [base[i] for i in range(4)], ns.value, ne.value
+
+
+class Batch:
+    """Many independent FP32 problems advanced together (dg_batch_*)."""
+
+    def __init__(self, cfgs, matrix_file: str | None = None, coeff_file: str | None = None):
+        n = len(cfgs)
+        arr = (DgParams * max(n, 1))()
+        dts = (C.c_double * max(n, 1))()
+        steps = (C.c_int * max(n, 1))()
+        for k, cfg in enumerate(cfgs):
+            p = params_from_dict(cfg) if isinstance(cfg, dict) else cfg
+            p.precision = DG_PRECISION_FP32
+            arr[k] = p
+            dts[k] = float(cfg["DT"])
+            steps[k] = int(cfg.get("STEPS", 1 << 30))
+        h = C.c_void_p()
+        _check(lib().dg_batch_create(n, arr, dts, steps, _b(matrix_file), _b(coeff_file), C.byref(h)),
+               "dg_batch_create")
+        self.h = h
+        self.n = n
+
+    h = None
+
+    def close(self):
+        if self.h:
+            lib().dg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def step(self, nsteps: int = 1):
+        _check(lib().dg_batch_step(self.h, int(nsteps)), "dg_batch_step")
+
+    def synchronize(self):
+        _check(lib().dg_batch_synchronize(self.h), "dg_batch_synchronize")
+
+    def info(self, i: int):
+        dims = (C.c_int * 3)()
+        sd = C.c_longlong()
+        t = C.c_double()
+        _check(lib().dg_batch_info(self.h, i, dims, C.byref(sd), C.byref(t)), "dg_batch_info")
+        return tuple(dims), sd.value, t.value
+
+    def state(self, i: int):
+        dims, _, _ = self.info(i)
+        rho = np.empty(dims)
+        vel = np.empty((3,) + dims)
+        _check(lib().dg_batch_get_state(self.h, i, _ptr(rho), _ptr(vel)), "dg_batch_get_state")
+        return rho, vel
+
+    @property
+    def total_nodes(self) -> int:
+        return lib().dg_batch_total_nodes(self.h)
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(lib().dg_batch_stream(self.h, C.byref(s)), "dg_batch_stream")
+        return s.value or 0
+
+    @property
+    def launches(self) -> int:
+        return lib().dg_batch_launch_count(self.h)
+
+    def autotune(self, trial_steps: int = 3) -> str:
+        buf = C.create_string_buffer(1024)
+        _check(lib().dg_batch_autotune(self.h, int(trial_steps), buf, 1024), "dg_batch_autotune")
+        return buf.value.decode()
+
+
+class Server:
+    """Continuous-batching request loop under an HBM budget (dg_serve_*)."""
+
+    def __init__(self, hbm_budget_bytes: int, keep_results: bool = False):
+        h = C.c_void_p()
+        _check(lib().dg_serve_create(int(hbm_budget_bytes), int(keep_results), C.byref(h)), "dg_serve_create")
+        self.h = h
+        self.dims = {}
+
+    h = None
+
+    def close(self):
+        if self.h:
+            lib().dg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def clock(self) -> float:
+        return lib().dg_serve_clock(self.h)
+
+    def submit(self, cfg: dict, arrival_time: float = -1.0) -> int:
+        p = params_from_dict(cfg)
+        rid = C.c_longlong()
+        _check(lib().dg_serve_submit(self.h, C.byref(p), float(cfg["DT"]), int(cfg["STEPS"]), float(arrival_time),
+                                     C.byref(rid)), "dg_serve_submit")
+        K = int(cfg["ORDER"]) + 1
+        nb = cfg.get("NUM_BLOCKS", [1, 1, 1])
+        self.dims[rid.value] = tuple(int(e) * int(b) * K for e, b in zip(cfg["NUM_ELEMENTS"], nb))
+        return rid.value
+
+    def tick(self) -> int:
+        n = C.c_int()
+        _check(lib().dg_serve_tick(self.h, C.byref(n)), "dg_serve_tick")
+        return n.value
+
+    def run(self, max_seconds: float = 0.0):
+        _check(lib().dg_serve_run(self.h, float(max_seconds)), "dg_serve_run")
+
+    def result(self, rid: int, state: bool = False):
+        ta, tadm, td = C.c_double(), C.c_double(), C.c_double()
+        rho = vel = None
+        if state:
+            dims = self.dims[rid]
+            rho = np.empty(dims)
+            vel = np.empty((3,) + dims)
+        _check(lib().dg_serve_result(self.h, rid, C.byref(ta), C.byref(tadm), C.byref(td), _ptr(rho), _ptr(vel)),
+               "dg_serve_result")
+        out = {"arrival": ta.value, "admit": tadm.value, "done": td.value}
+        if state:
+            out["rho"], out["vel"] = rho, vel
+        return out
+
+    def stats(self):
+        n, p50, p99, sps, mi = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        _check(lib().dg_serve_stats(self.h, C.byref(n), C.byref(p50), C.byref(p99), C.byref(sps), C.byref(mi)),
+               "dg_serve_stats")
+        return {"completed": n.value, "p50_s": p50.value, "p99_s": p99.value, "solves_per_s": sps.value,
+                "mean_inflight": mi.value}
 
 
 def line_operators(order: int, lumped: bool = False, matrix_file=None, coeff_file=None):

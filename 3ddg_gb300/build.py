@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "-I" + INCLUDE, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_CU = ["dg_solver.cu", "dg_noalloc.cu"]
+LIB_CU = ["dg_solver.cu", "dg_noalloc.cu", "batch.cu", "serve.cu"]
 LIB_CPP = ["basis.cpp", "mesh.cpp", "params.cpp", "h5lite.cpp", "snapshot.cpp"]
 DRIVER_CPP = ["host/Basis.cpp", "host/Grid.cpp", "host/HDF5Functions.cpp", "host/driver.cpp"]
 

@@ -1,0 +1,608 @@
+// Batched form (dg_batch_*): many independent FP32 problems of uneven
+// element counts and orders advanced together by the persistent stage kernel
+// of batch_kernels.cuh, one captured CUDA graph per RK step, tile sizes chosen
+// per order by an autotuner.  The serving form (serve.cu) drives the same
+// object, adding and removing problems as requests arrive and finish.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "batch_internal.h"
+#include "batch_kernels.cuh"
+#include "dg3d.h"
+#include "dg_kernels.cuh"
+#include "mesh.h"
+#include "solver_internal.h"
+
+namespace dg {
+
+#define DGB_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t _e = (call);                                                               \
+        if (_e != cudaSuccess)                                                                 \
+            return fail(DG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));    \
+    } while (0)
+
+size_t batch_problem_bytes(const dg_params& p)
+{
+    const int K = p.order + 1;
+    const size_t np = (size_t)(K * K * K + 7) / 8 * 8;
+    size_t ne = 1;
+    for (int a = 0; a < 3; a++) ne *= (size_t)p.num_blocks[a] * p.num_elements[a];
+    return ne * np * 23 * sizeof(float) + ne * (6 * sizeof(int) + sizeof(float));
+}
+
+namespace {
+
+template <int K>
+void fill_ops(BatchProblem& P, const LineOperators& op, const dg_params& p)
+{
+    const double w1[3] = {1.0, 1.0, 1.0};
+    const OpConst<double, K> C =
+        make_stage_const<double, K>(1.0, op.deriv.data(), op.lift0.data(), op.liftN.data(), w1, p.rho0, p.c0,
+                                    p.b_over_a, p.diff_const);
+    for (int i = 0; i < K; i++) {
+        for (int j = 0; j < K; j++) P.D[i][j] = (float)op.deriv[i * K + j];
+        P.L0[i] = (float)op.lift0[i];
+        P.LN[i] = (float)op.liftN[i];
+    }
+    for (int s = 0; s < 2; s++)
+        for (int i = 0; i < 4; i++) {
+            P.cM[s][i] = (float)C.cM[0][s][i];
+            P.cA[s][i] = (float)C.cA[0][s][i];
+        }
+    P.k1 = (float)C.k1;
+    P.k2 = (float)C.k2;
+    P.r0 = (float)C.r0;
+    P.inv_c2 = (float)C.inv_c2;
+    P.inv_z = (float)C.inv_z;
+    P.linear_mass = C.linear_mass;
+}
+
+}  // namespace
+
+std::string Batch::validate(const dg_params& p)
+{
+    std::string err = validate_params(p);
+    if (!err.empty()) return err;
+    if (p.order > BATCH_KMAX - 1) return "the batched form supports ORDER 1.." + std::to_string(BATCH_KMAX - 1);
+    return "";
+}
+
+int Batch::init(int device_capacity)
+{
+    DGB_CUDA(cudaGetDevice(&device));
+    DGB_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    cudaDeviceProp prop;
+    DGB_CUDA(cudaGetDeviceProperties(&prop, device));
+    num_sms = prop.multiProcessorCount;
+    int occ = 0;
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel, BATCH_THREADS, 0));
+    max_ctas_per_sm = std::max(1, occ);
+    ctas_per_sm = max_ctas_per_sm;
+    capacity = std::max(1, device_capacity);
+    DGB_CUDA(cudaMalloc(&d_probs, capacity * sizeof(BatchProblem)));
+    DGB_CUDA(cudaMalloc(&d_counters, 6 * sizeof(int)));
+    for (int k = 0; k <= BATCH_KMAX; k++) passes[k] = 4;
+    return DG_OK;
+}
+
+int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file, const char* coeff_file, int* index)
+{
+    std::string err = validate(p);
+    if (!err.empty()) return fail(DG_ERR_INVALID, err);
+    if (!(dt > 0.0) || steps < 1) return fail(DG_ERR_INVALID, "batch: dt must be > 0 and steps >= 1");
+    if ((int)probs.size() >= capacity) {
+        // grow the descriptor array
+        int ncap = capacity * 2;
+        BatchProblem* nd = nullptr;
+        DGB_CUDA(cudaMalloc(&nd, ncap * sizeof(BatchProblem)));
+        DGB_CUDA(cudaMemcpyAsync(nd, d_probs, probs.size() * sizeof(BatchProblem), cudaMemcpyDeviceToDevice, stream));
+        DGB_CUDA(cudaStreamSynchronize(stream));
+        cudaFree(d_probs);
+        d_probs = nd;
+        capacity = ncap;
+    }
+    LineOperators op;
+    const std::string key = std::to_string(p.order) + "|" + std::to_string(p.lumped_mass) + "|" +
+                            (matrix_file ? matrix_file : "") + "|" + (coeff_file ? coeff_file : "");
+    auto it = op_cache.find(key);
+    if (it == op_cache.end()) {
+        err = build_line_operators(p.order, p.lumped_mass != 0, matrix_file ? matrix_file : "",
+                                   coeff_file ? coeff_file : "", op);
+        if (!err.empty()) return fail(err.find("Opening") == 0 ? DG_ERR_IO : DG_ERR_INVALID, err);
+        op_cache[key] = op;
+    } else {
+        op = it->second;
+    }
+    MeshHost m;
+    err = build_mesh(p, op, m);
+    if (!err.empty()) return fail(DG_ERR_INVALID, err);
+
+    Entry E;
+    E.p = p;
+    E.dt = dt;
+    E.steps = steps;
+    E.K = m.K;
+    E.np = m.NP;
+    E.n_elem = m.n_elem;
+    for (int a = 0; a < 3; a++) E.dims[a] = m.E[a] * m.K;
+    E.fs = m.fstride();
+    E.nb[0] = m.nb[0]; E.nb[1] = m.nb[1]; E.nb[2] = m.nb[2];
+    E.ne[0] = m.ne[0]; E.ne[1] = m.ne[1]; E.ne[2] = m.ne[2];
+    const size_t bytes = E.fs * 23 * sizeof(float);
+    DGB_CUDA(cudaMalloc(&E.data, bytes));
+    DGB_CUDA(cudaMemsetAsync(E.data, 0, bytes, stream));
+    std::vector<int> nbr(m.nbr.size());
+    for (size_t i = 0; i < m.nbr.size(); i++) nbr[i] = m.nbr[i] >= 0 ? m.nbr[i] : -1 - m.bnd_face[-1 - m.nbr[i]];
+    DGB_CUDA(cudaMalloc(&E.nbr, nbr.size() * sizeof(int)));
+    DGB_CUDA(cudaMemcpyAsync(E.nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    std::vector<float> sg(m.sigma.begin(), m.sigma.end());
+    DGB_CUDA(cudaMalloc(&E.sigma, sg.size() * sizeof(float)));
+    DGB_CUDA(cudaMemcpyAsync(E.sigma, sg.data(), sg.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+    std::vector<float> s0(m.state0.begin(), m.state0.end());
+    DGB_CUDA(cudaMemcpyAsync(E.data, s0.data(), s0.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+
+    BatchProblem& P = E.desc;
+    std::memset(&P, 0, sizeof P);
+    P.K = m.K;
+    P.np = m.NP;
+    P.n_elem = m.n_elem;
+    P.src_face = p.src_face;
+    P.active = 1;
+    P.cur = 0;
+    P.steps_left = steps;
+    float* base = (float*)E.data;
+    P.u[0] = base;
+    P.u[1] = base + 4 * E.fs;
+    P.comp = base + 8 * E.fs;
+    P.d[0] = base + 12 * E.fs;
+    P.d[1] = base + 16 * E.fs;
+    P.q = base + 20 * E.fs;
+    P.nbr = E.nbr;
+    P.sigma = E.sigma;
+    P.fs = E.fs;
+    switch (m.K) {
+    case 2: fill_ops<2>(P, op, p); break;
+    case 3: fill_ops<3>(P, op, p); break;
+    case 4: fill_ops<4>(P, op, p); break;
+    case 5: fill_ops<5>(P, op, p); break;
+    case 6: fill_ops<6>(P, op, p); break;
+    }
+    for (int a = 0; a < 3; a++) {
+        P.invw[a] = (float)(1.0 / p.elem_width[a]);
+        P.gscale[a] = (float)(p.eval_diff ? p.diff_const / p.elem_width[a] : 0.0);
+    }
+    const double w23 = p.rk_exact ? 2.0 / 3.0 : (double)(2.0f / 3.0f);
+    const double w13 = p.rk_exact ? 1.0 / 3.0 : (double)(1.0f / 3.0f);
+    P.ca[0] = (float)dt;
+    P.ca[1] = (float)(dt * .25);
+    P.ca[2] = (float)(dt * 2.0 / 3.0);
+    P.cb[0] = 0.f;
+    P.cb[1] = .25f;
+    P.cb[2] = (float)w23;
+    P.eps = (float)(w23 + w13 - 1.0);
+    if (!p.eval_advect) {
+        P.k1 = P.k2 = 0.f;
+        P.r0 = 0.f;
+        P.linear_mass = 1;
+        std::memset(P.cM, 0, sizeof P.cM);
+        std::memset(P.cA, 0, sizeof P.cA);
+    }
+    P.t = 0.0;
+    P.dt = dt;
+    P.src_amp = p.src_amp;
+    P.src_freq = p.src_freq;
+    P.src_T = p.src_face >= 0 ? p.src_cycles / p.src_freq : 0.0;
+    P.src_phase = p.src_phase;
+    E.id = next_id++;
+    probs.push_back(E);
+    DGB_CUDA(cudaMemcpyAsync(d_probs + probs.size() - 1, &P, sizeof P, cudaMemcpyHostToDevice, stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    if (index) *index = (int)probs.size() - 1;
+    tiles_dirty = true;
+    return DG_OK;
+}
+
+int Batch::remove(int i)
+{
+    if (i < 0 || i >= (int)probs.size()) return fail(DG_ERR_INVALID, "batch: bad problem index");
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    Entry& E = probs[i];
+    cudaFree(E.data);
+    cudaFree(E.nbr);
+    cudaFree(E.sigma);
+    probs.erase(probs.begin() + i);
+    // re-pack the descriptor array (host copies are authoritative except the
+    // time-dependent fields, which are read back first)
+    std::vector<BatchProblem> h(probs.size());
+    for (size_t j = 0; j < probs.size(); j++) h[j] = probs[j].desc;
+    if (!h.empty()) {
+        // pull the live descriptors of the kept problems, in their old slots
+        std::vector<BatchProblem> live(probs.size() + 1);
+        DGB_CUDA(cudaMemcpy(live.data(), d_probs, (probs.size() + 1) * sizeof(BatchProblem), cudaMemcpyDeviceToHost));
+        for (size_t j = 0; j < probs.size(); j++) h[j] = live[j < (size_t)i ? j : j + 1];
+        DGB_CUDA(cudaMemcpy(d_probs, h.data(), h.size() * sizeof(BatchProblem), cudaMemcpyHostToDevice));
+    }
+    tiles_dirty = true;
+    return DG_OK;
+}
+
+void Batch::build_tiles()
+{
+    tiles.clear();
+    // largest orders first: the atomic tile counter then hands out the
+    // longest tiles early and the short ones fill the tail
+    std::vector<int> order(probs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return probs[a].K > probs[b].K; });
+    for (int i : order) {
+        const Entry& E = probs[i];
+        const int K = E.K;
+        const int chunk = bepb_of(K) * std::max(1, passes[K]);
+        for (int e0 = 0; e0 < E.n_elem; e0 += chunk) {
+            BatchTile t;
+            t.prob = i;
+            t.e0 = e0;
+            t.count = std::min(chunk, E.n_elem - e0);
+            t.K = K;
+            tiles.push_back(t);
+        }
+    }
+}
+
+int Batch::upload_tiles()
+{
+    build_tiles();
+    if ((int)tiles.size() > tile_capacity) {
+        if (d_tiles) cudaFree(d_tiles);
+        tile_capacity = std::max<int>((int)tiles.size(), 2 * tile_capacity);
+        DGB_CUDA(cudaMalloc(&d_tiles, tile_capacity * sizeof(BatchTile)));
+    }
+    if (!tiles.empty())
+        DGB_CUDA(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
+                                 stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    tiles_dirty = false;
+    if (graph) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    return DG_OK;
+}
+
+int Batch::launch_step()
+{
+    const int n = (int)probs.size();
+    DGB_CUDA(cudaMemsetAsync(d_counters, 0, 6 * sizeof(int), stream));
+    batch_step_begin<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
+    for (int s = 0; s < 3; s++) {
+        BatchArgs A;
+        A.probs = d_probs;
+        A.tiles = d_tiles;
+        A.n_tiles = (int)tiles.size();
+        A.counters = d_counters + 2 * s;
+        A.stage = s;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(num_sms * ctas_per_sm);
+        cfg.blockDim = dim3(BATCH_THREADS);
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        DGB_CUDA(cudaLaunchKernelEx(&cfg, batch_stage_kernel, A));
+    }
+    batch_step_end<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
+    DGB_CUDA(cudaGetLastError());
+    launches += 5;
+    return DG_OK;
+}
+
+int Batch::step(int nsteps)
+{
+    if (probs.empty()) return DG_OK;
+    if (tiles_dirty) {
+        int rc = upload_tiles();
+        if (rc) return rc;
+    }
+    if (use_graph && !graph) {
+        cudaGraph_t g = nullptr;
+        DGB_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_step();
+        cudaError_t ec = cudaStreamEndCapture(stream, &g);
+        if (rc || ec != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            use_graph = false;  // capture unsupported here: launch directly
+        } else {
+            cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                graph = nullptr;
+                use_graph = false;
+                cudaGetLastError();
+            }
+        }
+    }
+    for (int i = 0; i < nsteps; i++) {
+        if (graph) {
+            DGB_CUDA(cudaGraphLaunch(graph, stream));
+            launches += 5;
+        } else {
+            int rc = launch_step();
+            if (rc) return rc;
+        }
+    }
+    return DG_OK;
+}
+
+int Batch::sync_descs()
+{
+    std::vector<BatchProblem> h(probs.size());
+    if (h.empty()) return DG_OK;
+    DGB_CUDA(cudaMemcpyAsync(h.data(), d_probs, h.size() * sizeof(BatchProblem), cudaMemcpyDeviceToHost, stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < h.size(); i++) probs[i].desc = h[i];
+    return DG_OK;
+}
+
+int Batch::get_state(int i, double* drho, double* vel)
+{
+    if (i < 0 || i >= (int)probs.size()) return fail(DG_ERR_INVALID, "batch: bad problem index");
+    int rc = sync_descs();
+    if (rc) return rc;
+    Entry& E = probs[i];
+    const size_t g = (size_t)E.n_elem * E.K * E.K * E.K;
+    double* st = nullptr;
+    DGB_CUDA(cudaMallocAsync(&st, 4 * g * sizeof(double), stream));
+    GridMap gm;
+    gm.K = E.K;
+    for (int a = 0; a < 3; a++) {
+        gm.nb[a] = E.nb[a];
+        gm.ne[a] = E.ne[a];
+        gm.E[a] = E.nb[a] * E.ne[a];
+    }
+    gm.elem_per_block = E.ne[0] * E.ne[1] * E.ne[2];
+    const float* u = E.desc.u[E.desc.cur];
+    pack_grid_kernel<float><<<304, 256, 0, stream>>>(u, E.fs, E.np, 4, gm, E.n_elem, st, g);
+    DGB_CUDA(cudaGetLastError());
+    if (drho) DGB_CUDA(cudaMemcpyAsync(drho, st, g * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (vel) DGB_CUDA(cudaMemcpyAsync(vel, st + g, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    DGB_CUDA(cudaFreeAsync(st, stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    return DG_OK;
+}
+
+// Save / restore of every problem's time-dependent data, for the autotuner.
+int Batch::snapshot(std::vector<std::vector<char>>& save)
+{
+    int rc = sync_descs();
+    if (rc) return rc;
+    save.resize(probs.size());
+    for (size_t i = 0; i < probs.size(); i++) {
+        const size_t bytes = probs[i].fs * 23 * sizeof(float);
+        save[i].resize(bytes);
+        DGB_CUDA(cudaMemcpyAsync(save[i].data(), probs[i].data, bytes, cudaMemcpyDeviceToHost, stream));
+    }
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    saved_desc.resize(probs.size());
+    for (size_t i = 0; i < probs.size(); i++) saved_desc[i] = probs[i].desc;
+    return DG_OK;
+}
+
+int Batch::restore(const std::vector<std::vector<char>>& save)
+{
+    for (size_t i = 0; i < probs.size(); i++)
+        DGB_CUDA(cudaMemcpyAsync(probs[i].data, save[i].data(), save[i].size(), cudaMemcpyHostToDevice, stream));
+    DGB_CUDA(cudaMemcpyAsync(d_probs, saved_desc.data(), saved_desc.size() * sizeof(BatchProblem),
+                             cudaMemcpyHostToDevice, stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < probs.size(); i++) probs[i].desc = saved_desc[i];
+    return DG_OK;
+}
+
+int Batch::time_steps(int n, double* ms)
+{
+    cudaEvent_t a, b;
+    DGB_CUDA(cudaEventCreate(&a));
+    DGB_CUDA(cudaEventCreate(&b));
+    int rc = step(1);  // warm: uploads, graph capture
+    if (rc) return rc;
+    DGB_CUDA(cudaEventRecord(a, stream));
+    rc = step(n);
+    if (rc) return rc;
+    DGB_CUDA(cudaEventRecord(b, stream));
+    DGB_CUDA(cudaEventSynchronize(b));
+    float t = 0.f;
+    DGB_CUDA(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t / n;
+    return DG_OK;
+}
+
+// Coordinate descent over the per-order tile size (passes of EPB elements per
+// tile) and the persistent grid (CTAs per SM), timing real steps of this
+// batch; the state is saved before and restored after.
+int Batch::autotune(int trial_steps, std::string& report)
+{
+    if (probs.empty()) return DG_OK;
+    std::vector<std::vector<char>> save;
+    int rc = snapshot(save);
+    if (rc) return rc;
+    std::vector<int> orders;
+    for (const Entry& E : probs)
+        if (std::find(orders.begin(), orders.end(), E.K) == orders.end()) orders.push_back(E.K);
+    std::sort(orders.begin(), orders.end());
+    const int cand_pass[] = {1, 2, 4, 8, 16};
+    double best = 0;
+    tiles_dirty = true;
+    rc = time_steps(trial_steps, &best);
+    if (rc) return rc;
+    report.clear();
+    for (int round = 0; round < 2; round++) {
+        for (int K : orders) {
+            int keep = passes[K];
+            for (int c : cand_pass) {
+                if (c == keep) continue;
+                passes[K] = c;
+                tiles_dirty = true;
+                double ms;
+                if ((rc = restore(save))) return rc;
+                if ((rc = time_steps(trial_steps, &ms))) return rc;
+                if (ms < best * 0.995) {
+                    best = ms;
+                    keep = c;
+                }
+            }
+            passes[K] = keep;
+        }
+        int keep_c = ctas_per_sm;
+        for (int c = 1; c <= max_ctas_per_sm; c++) {
+            if (c == keep_c) continue;
+            ctas_per_sm = c;
+            if (graph) {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+            }
+            double ms;
+            if ((rc = restore(save))) return rc;
+            if ((rc = time_steps(trial_steps, &ms))) return rc;
+            if (ms < best * 0.995) {
+                best = ms;
+                keep_c = c;
+            }
+        }
+        ctas_per_sm = keep_c;
+    }
+    tiles_dirty = true;
+    if ((rc = restore(save))) return rc;
+    if ((rc = upload_tiles())) return rc;
+    for (int K : orders) report += "K=" + std::to_string(K) + ":elems_per_tile=" + std::to_string(bepb_of(K) * passes[K]) + " ";
+    report += "ctas_per_sm=" + std::to_string(ctas_per_sm) + " ms_per_step=" + std::to_string(best);
+    return DG_OK;
+}
+
+size_t Batch::total_nodes() const
+{
+    size_t n = 0;
+    for (const Entry& E : probs) n += (size_t)E.n_elem * E.K * E.K * E.K;
+    return n;
+}
+
+Batch::~Batch()
+{
+    if (stream) cudaStreamSynchronize(stream);
+    if (graph) cudaGraphExecDestroy(graph);
+    for (Entry& E : probs) {
+        cudaFree(E.data);
+        cudaFree(E.nbr);
+        cudaFree(E.sigma);
+    }
+    if (d_probs) cudaFree(d_probs);
+    if (d_tiles) cudaFree(d_tiles);
+    if (d_counters) cudaFree(d_counters);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+}  // namespace dg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct dg_batch {
+    dg::Batch b;
+};
+
+extern "C" {
+
+int dg_batch_create(int n, const dg_params* params, const double* dt, const int* steps, const char* matrix_file,
+                    const char* coeff_file, dg_batch** out)
+{
+    if (!out || n < 0 || (n > 0 && (!params || !dt || !steps)))
+        return dg::fail(DG_ERR_INVALID, "dg_batch_create: bad argument");
+    *out = nullptr;
+    dg_batch* h = new (std::nothrow) dg_batch;
+    if (!h) return dg::fail(DG_ERR_NOMEM, "dg_batch_create: host allocation failed");
+    int rc = h->b.init(std::max(n, 16));
+    for (int i = 0; rc == DG_OK && i < n; i++) rc = h->b.add(params[i], dt[i], steps[i], matrix_file, coeff_file, nullptr);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return DG_OK;
+}
+
+int dg_batch_destroy(dg_batch* b)
+{
+    delete b;
+    return DG_OK;
+}
+
+int dg_batch_step(dg_batch* b, int nsteps)
+{
+    if (!b || nsteps < 0) return dg::fail(DG_ERR_INVALID, "dg_batch_step: bad argument");
+    return b->b.step(nsteps);
+}
+
+int dg_batch_synchronize(dg_batch* b)
+{
+    if (!b) return dg::fail(DG_ERR_INVALID, "dg_batch_synchronize: null handle");
+    cudaError_t e = cudaStreamSynchronize(b->b.stream);
+    if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    return DG_OK;
+}
+
+int dg_batch_get_state(dg_batch* b, int i, double* drho, double* vel)
+{
+    if (!b) return dg::fail(DG_ERR_INVALID, "dg_batch_get_state: null handle");
+    return b->b.get_state(i, drho, vel);
+}
+
+int dg_batch_info(dg_batch* b, int i, int* dims3, long long* steps_done, double* time)
+{
+    if (!b || i < 0 || i >= (int)b->b.probs.size()) return dg::fail(DG_ERR_INVALID, "dg_batch_info: bad argument");
+    int rc = b->b.sync_descs();
+    if (rc) return rc;
+    const dg::Batch::Entry& E = b->b.probs[i];
+    if (dims3)
+        for (int a = 0; a < 3; a++) dims3[a] = E.dims[a];
+    if (steps_done) *steps_done = E.desc.steps_done;
+    if (time) *time = E.desc.t;
+    return DG_OK;
+}
+
+long long dg_batch_total_nodes(const dg_batch* b) { return b ? (long long)b->b.total_nodes() : 0; }
+
+int dg_batch_autotune(dg_batch* b, int trial_steps, char* report, size_t report_len)
+{
+    if (!b || trial_steps < 1) return dg::fail(DG_ERR_INVALID, "dg_batch_autotune: bad argument");
+    std::string r;
+    int rc = b->b.autotune(trial_steps, r);
+    if (rc) return rc;
+    if (report && report_len) {
+        std::strncpy(report, r.c_str(), report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    return DG_OK;
+}
+
+int dg_batch_stream(dg_batch* b, void** stream)
+{
+    if (!b || !stream) return dg::fail(DG_ERR_INVALID, "dg_batch_stream: null argument");
+    *stream = (void*)b->b.stream;
+    return DG_OK;
+}
+
+long long dg_batch_launch_count(const dg_batch* b) { return b ? b->b.launches : 0; }
+
+}  // extern "C"

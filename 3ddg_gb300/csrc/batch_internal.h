@@ -1,0 +1,74 @@
+// Internal state of a batch of independent FP32 problems (dg_batch_*), shared
+// by batch.cu and serve.cpp; not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "basis.h"
+#include "batch_types.h"
+#include "dg3d.h"
+
+namespace dg {
+
+// Device bytes one problem of the batched form holds (state, stages,
+// compensation, gradient, face table, sigma).
+size_t batch_problem_bytes(const dg_params& p);
+
+struct Batch {
+    struct Entry {
+        dg_params p;
+        double dt = 0.0;
+        int steps = 0;
+        int K = 0, np = 0, n_elem = 0;
+        int dims[3] = {0, 0, 0};
+        int nb[3] = {1, 1, 1}, ne[3] = {1, 1, 1};
+        size_t fs = 0;
+        void* data = nullptr;  // 23 float fields: u0, u1, comp, d1, d2 (4 each), q (3)
+        int* nbr = nullptr;
+        float* sigma = nullptr;
+        BatchProblem desc;     // host copy of the device descriptor
+        long long id = 0;
+    };
+
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0, max_ctas_per_sm = 1, ctas_per_sm = 1;
+    int passes[BATCH_KMAX + 1];  // autotuned: passes of EPB(K) elements per tile
+    std::vector<Entry> probs;
+    std::vector<BatchProblem> saved_desc;
+    std::map<std::string, LineOperators> op_cache;
+    BatchProblem* d_probs = nullptr;
+    int capacity = 0;
+    std::vector<BatchTile> tiles;
+    BatchTile* d_tiles = nullptr;
+    int tile_capacity = 0;
+    int* d_counters = nullptr;
+    bool tiles_dirty = true;
+    bool use_graph = true;
+    cudaGraphExec_t graph = nullptr;
+    long long launches = 0;
+    long long next_id = 1;
+
+    static std::string validate(const dg_params& p);
+    int init(int device_capacity);
+    int add(const dg_params& p, double dt, int steps, const char* matrix_file, const char* coeff_file, int* index);
+    int remove(int i);
+    void build_tiles();
+    int upload_tiles();
+    int launch_step();
+    int step(int nsteps);
+    int sync_descs();
+    int get_state(int i, double* drho, double* vel);
+    int snapshot(std::vector<std::vector<char>>& save);
+    int restore(const std::vector<std::vector<char>>& save);
+    int time_steps(int n, double* ms);
+    int autotune(int trial_steps, std::string& report);
+    size_t total_nodes() const;
+    ~Batch();
+};
+
+}  // namespace dg

@@ -1,0 +1,295 @@
+// Batched form: many independent problems of uneven element counts and
+// orders advanced together, FP32 fields/fluxes/stages with the
+// Kahan-compensated update, one persistent kernel per RK stage.
+//
+// Each problem keeps its own device buffers and a device descriptor
+// (BatchProblem) with its FP32 operators, RK weights, time and source state,
+// so problems can join and leave (the serving form) without touching the
+// others.  A stage launch is a cooperative persistent grid that pulls tiles
+// (problem, first element, element count) from a work list with an atomic
+// counter: phase 1 computes the LDG gradient of every tile, a grid-wide
+// barrier, phase 2 the stage update of every tile.  A tile runs the code path
+// of its problem's order (K = N + 1 <= 6) with EPB(K) elements per pass of a
+// 256-thread CTA; the number of passes per tile (tile size) is chosen per
+// order by the autotuner.  The arithmetic per element is the one of
+// stage_kernel / ldg_gradient_kernel (dg_kernels.cuh) with 1/w_a applied after
+// the line sums, so one descriptor serves all three stages.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "batch_types.h"
+#include "dg_kernels.cuh"
+
+namespace dg {
+
+__host__ __device__ constexpr int bepb_of(int K) { return BATCH_THREADS / npt_of(K); }
+
+__device__ __forceinline__ void batch_exterior(const BatchProblem& P, int face, int stage, float& ro, float& uo)
+{
+    if (face == P.src_face) {
+        const float p = P.src_p[stage];
+        ro = p * P.inv_c2;
+        uo = ((face & 1) ? -p : p) * P.inv_z;
+    } else {
+        ro = 0.f;
+        uo = 0.f;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ float batch_in(const BatchProblem& P, const float* ub, const float* inc, int f, size_t off)
+{
+    float v = __ldg(ub + (size_t)f * P.fs + off);
+    if (inc) v += __ldg(inc + (size_t)f * P.fs + off);
+    return v;
+}
+
+template <int K>
+__device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
+{
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
+    GradSmem<float, K>* SM = reinterpret_cast<GradSmem<float, K>*>(smraw);
+    const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
+    const int c[3] = {n / K2, (n / K) % K, n % K};
+    const float* ub = P.u[P.cur];
+    const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
+    for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
+        const int e = c0 + slot;
+        const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
+        GradSmem<float, K>& S = SM[slot < EPB ? slot : 0];
+        float rho = 0.f;
+        if (act) rho = batch_in<K>(P, ub, inc, 0, (size_t)e * P.np + n);
+        if (slot < EPB) S.r[n] = rho;
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (c[a] != 0 && c[a] != K - 1) continue;
+                const int side = c[a] == 0 ? 0 : 1;
+                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                const int code = __ldg(P.nbr + (size_t)e * 6 + 2 * a + side);
+                float ro, uo;
+                if (code >= 0) {
+                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+                    ro = batch_in<K>(P, ub, inc, 0, (size_t)code * P.np + nn);
+                } else {
+                    batch_exterior(P, -1 - code, stage, ro, uo);
+                }
+                S.fl[a][side][fi] = (side ? -0.5f : 0.5f) * (ro + rho);
+            }
+        }
+        __syncthreads();
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
+                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                float s = P.L0[ia] * S.fl[a][0][fi];
+                s += P.LN[ia] * S.fl[a][1][fi];
+#pragma unroll
+                for (int j = 0; j < K; j++) s += P.D[ia][j] * S.r[base + j * st];
+                P.q[(size_t)a * P.fs + (size_t)e * P.np + n] = P.gscale[a] * s;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int K>
+__device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
+{
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
+    StageSmem<float, K>* SM = reinterpret_cast<StageSmem<float, K>*>(smraw);
+    const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
+    const int c[3] = {n / K2, (n / K) % K, n % K};
+    const float* ub = P.u[P.cur];
+    const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
+    const bool final_stage = stage == 2;
+    float* dout = final_stage ? P.u[P.cur ^ 1] : P.d[stage];
+    const float ca = P.ca[stage], cb = P.cb[stage], eps = final_stage ? P.eps : 0.f;
+    for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
+        const int e = c0 + slot;
+        const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
+        StageSmem<float, K>& S = SM[slot < EPB ? slot : 0];
+        const size_t off = (size_t)e * P.np + n;
+        float rho = 0.f, u[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
+        if (act) {
+            rho = batch_in<K>(P, ub, inc, 0, off);
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                u[a] = batch_in<K>(P, ub, inc, 1 + a, off);
+                q[a] = __ldg(P.q + (size_t)a * P.fs + off);
+            }
+        }
+        const float fmom = momentum_flux(rho, P.k1, P.k2);
+        float fmass[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, P.r0, P.linear_mass);
+        if (slot < EPB) {
+            S.fm[n] = fmom;
+#pragma unroll
+            for (int a = 0; a < 3; a++) S.fh[a][n] = fmass[a] + q[a];
+        }
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (c[a] != 0 && c[a] != K - 1) continue;
+                const int side = c[a] == 0 ? 0 : 1;
+                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                const int code = __ldg(P.nbr + (size_t)e * 6 + 2 * a + side);
+                float ro, uo, qo = 0.f;
+                if (code >= 0) {
+                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+                    const size_t o2 = (size_t)code * P.np + nn;
+                    ro = batch_in<K>(P, ub, inc, 0, o2);
+                    uo = batch_in<K>(P, ub, inc, 1 + a, o2);
+                    qo = __ldg(P.q + (size_t)a * P.fs + o2);
+                } else {
+                    batch_exterior(P, -1 - code, stage, ro, uo);
+                }
+                const float fmo = momentum_flux(ro, P.k1, P.k2);
+                const float fao = mass_flux(uo, ro, P.r0, P.linear_mass);
+                const float* cm = P.cM[side];
+                const float* cr = P.cA[side];
+                S.gm[a][side][fi] = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
+                S.gr[a][side][fi] = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3] +
+                                    (side ? -0.5f : 0.5f) * (qo + q[a]);
+            }
+        }
+        __syncthreads();
+        if (act) {
+            float r_rho = 0.f, r_u[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
+                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                float sr = P.L0[ia] * S.gr[a][0][fi];
+                sr += P.LN[ia] * S.gr[a][1][fi];
+                float sm = P.L0[ia] * S.gm[a][0][fi];
+                sm += P.LN[ia] * S.gm[a][1][fi];
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    const float dj = P.D[ia][j];
+                    sr += dj * S.fh[a][base + j * st];
+                    sm += dj * S.fm[base + j * st];
+                }
+                r_rho += P.invw[a] * sr;
+                r_u[a] = P.invw[a] * sm;
+            }
+            const float ks = ca * __ldg(P.sigma + e);
+            const float cbe = cb - ks, ce = eps - ks;
+            const float r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const size_t o = (size_t)f * P.fs + off;
+                const float ubv = __ldg(ub + o);
+                float d = ca * r[f] + ubv * ce;
+                if (inc) d += __ldg(inc + o) * cbe;
+                if (final_stage) {
+                    const float y = d - P.comp[o];
+                    const float t = ubv + y;
+                    P.comp[o] = (t - ubv) - y;
+                    dout[o] = t;
+                } else {
+                    dout[o] = d;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Shared memory of one CTA: the largest per-order need.
+__host__ __device__ constexpr size_t batch_smem_bytes()
+{
+    size_t m = 0;
+    const size_t s2 = bepb_of(2) * sizeof(StageSmem<float, 2>), s3 = bepb_of(3) * sizeof(StageSmem<float, 3>);
+    const size_t s4 = bepb_of(4) * sizeof(StageSmem<float, 4>), s5 = bepb_of(5) * sizeof(StageSmem<float, 5>);
+    const size_t s6 = bepb_of(6) * sizeof(StageSmem<float, 6>);
+    m = s2 > m ? s2 : m;
+    m = s3 > m ? s3 : m;
+    m = s4 > m ? s4 : m;
+    m = s5 > m ? s5 : m;
+    m = s6 > m ? s6 : m;
+    return m;
+}
+
+__device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProblem* src)
+{
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(BatchProblem) / sizeof(int)); i += blockDim.x) d[i] = s[i];
+}
+
+// One RK stage of every active problem: LDG gradient of every tile, grid
+// barrier, stage update of every tile.
+__global__ void __launch_bounds__(BATCH_THREADS, 4) batch_stage_kernel(BatchArgs A)
+{
+    __shared__ __align__(16) unsigned char smraw[batch_smem_bytes()];
+    __shared__ BatchProblem P;
+    __shared__ int tile_idx;
+    for (int phase = 0; phase < 2; phase++) {
+        if (phase == 1) cooperative_groups::this_grid().sync();
+        for (;;) {
+            if (threadIdx.x == 0) tile_idx = atomicAdd(A.counters + phase, 1);
+            __syncthreads();
+            const int ti = tile_idx;
+            if (ti >= A.n_tiles) break;
+            const BatchTile T = A.tiles[ti];
+            load_problem(P, A.probs + T.prob);
+            __syncthreads();
+            if (P.active) {
+                if (phase == 0) {
+                    switch (T.K) {
+                    case 2: batch_grad_tile<2>(P, T, A.stage, smraw); break;
+                    case 3: batch_grad_tile<3>(P, T, A.stage, smraw); break;
+                    case 4: batch_grad_tile<4>(P, T, A.stage, smraw); break;
+                    case 5: batch_grad_tile<5>(P, T, A.stage, smraw); break;
+                    case 6: batch_grad_tile<6>(P, T, A.stage, smraw); break;
+                    }
+                } else {
+                    switch (T.K) {
+                    case 2: batch_stage_tile<2>(P, T, A.stage, smraw); break;
+                    case 3: batch_stage_tile<3>(P, T, A.stage, smraw); break;
+                    case 4: batch_stage_tile<4>(P, T, A.stage, smraw); break;
+                    case 5: batch_stage_tile<5>(P, T, A.stage, smraw); break;
+                    case 6: batch_stage_tile<6>(P, T, A.stage, smraw); break;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Per-problem bookkeeping around a step (one thread per problem).
+__global__ void batch_step_begin(BatchProblem* probs, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BatchProblem& P = probs[i];
+    if (!P.active) return;
+    const double ts[3] = {P.t, P.t + P.dt, P.t + 0.5 * P.dt};
+    for (int s = 0; s < 3; s++) {
+        double p = 0.0;
+        if (P.src_face >= 0 && ts[s] >= 0.0 && ts[s] <= P.src_T) {
+            const double w = sin(3.14159265358979323846 * ts[s] / P.src_T);
+            p = P.src_amp * w * w * sin(2.0 * 3.14159265358979323846 * P.src_freq * ts[s] + P.src_phase);
+        }
+        P.src_p[s] = (float)p;
+    }
+}
+
+__global__ void batch_step_end(BatchProblem* probs, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BatchProblem& P = probs[i];
+    if (!P.active) return;
+    P.t += P.dt;
+    P.cur ^= 1;
+    P.steps_done++;
+    if (--P.steps_left <= 0) P.active = 0;
+}
+
+}  // namespace dg

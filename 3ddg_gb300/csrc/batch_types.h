@@ -1,0 +1,48 @@
+// Data types of the batched form shared by its host code (batch.cu,
+// serve.cu) and its kernels (batch_kernels.cuh).
+#pragma once
+
+#include <cstddef>
+
+namespace dg {
+
+constexpr int BATCH_THREADS = 256;
+constexpr int BATCH_KMAX = 6;
+
+struct BatchProblem {
+    int K, np, n_elem, src_face;
+    int active, cur, steps_left, pad;
+    float* u[2];           // ping-pong state, 4 fields each
+    float* comp;           // Kahan compensation
+    float* d[2];           // stage increments d1, d2
+    float* q;              // LDG gradient times -D_c, 3 fields
+    const int* nbr;        // n_elem x 6, problem-local; boundary: -1 - face
+    const float* sigma;    // n_elem
+    size_t fs;             // field stride n_elem * np
+    float D[BATCH_KMAX][BATCH_KMAX];
+    float L0[BATCH_KMAX], LN[BATCH_KMAX];
+    float invw[3];         // 1 / w_a
+    float gscale[3];       // D_c / w_a
+    float cM[2][4], cA[2][4];  // face coefficients with the lift scales, w factored out
+    float k1, k2, r0, inv_c2, inv_z;
+    int linear_mass;
+    float ca[3], cb[3], eps;   // R weight, increment weight, u weight of each stage
+    float src_p[3];        // source pressure at the three stage times of this step
+    double t, dt;
+    double src_amp, src_freq, src_T, src_phase;
+    long long steps_done;
+};
+
+struct BatchTile {
+    int prob, e0, count, K;
+};
+
+struct BatchArgs {
+    BatchProblem* probs;
+    const BatchTile* tiles;
+    int n_tiles;
+    int* counters;         // [2]: phase-1 and phase-2 tile counters, zeroed before the launch
+    int stage;
+};
+
+}  // namespace dg

@@ -262,8 +262,55 @@ int Solver::rk_stage_fp32(int s_idx, double dt, float* rhs_only)
     return DG_OK;
 }
 
+template <typename T>
+__global__ void probe_kernel(const T* __restrict__ state, size_t fs, const long long* __restrict__ off, int n,
+                             double* __restrict__ row, double c2, double kba)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = (double)state[off[i]];
+    row[i] = c2 * (d + kba * d * d);
+    (void)fs;
+}
+
+int Solver::probe_reserve(long long steps)
+{
+    if (n_probe == 0 || steps <= probe_cap) return DG_OK;
+    long long cap = std::max<long long>(steps, 2 * probe_cap + 64);
+    double* nb = nullptr;
+    DG_CUDA(cudaMalloc(&nb, (size_t)cap * n_probe * sizeof(double)));
+    if (d_probe_rec && probe_steps)
+        DG_CUDA(cudaMemcpyAsync(nb, d_probe_rec, (size_t)probe_steps * n_probe * sizeof(double),
+                                cudaMemcpyDeviceToDevice, stream));
+    DG_CUDA(cudaStreamSynchronize(stream));
+    if (d_probe_rec) cudaFree(d_probe_rec);
+    d_probe_rec = nb;
+    probe_cap = cap;
+    return DG_OK;
+}
+
+void Solver::probe_record()
+{
+    if (n_probe == 0) return;
+    const double c2 = p.c0 * p.c0, kba = p.b_over_a / (2.0 * p.rho0);
+    double* row = d_probe_rec + (size_t)probe_steps * n_probe;
+    if (fp64())
+        probe_kernel<double><<<(n_probe + 127) / 128, 128, 0, stream>>>((const double*)state_ptr(), mesh.fstride(),
+                                                                       d_probe_off, n_probe, row, c2, kba);
+    else
+        probe_kernel<float><<<(n_probe + 127) / 128, 128, 0, stream>>>((const float*)state_ptr(), mesh.fstride(),
+                                                                      d_probe_off, n_probe, row, c2, kba);
+    launches++;
+    probe_t.push_back(t);
+    probe_steps++;
+}
+
 int Solver::step(double dt, int nsteps)
 {
+    if (n_probe) {
+        int rc = probe_reserve(probe_steps + nsteps);
+        if (rc) return rc;
+    }
     for (int n = 0; n < nsteps; n++) {
         for (int s = 0; s < 3; s++) {
             int rc = fp64() ? rk_stage_fp64(s, dt, nullptr) : rk_stage_fp32(s, dt, nullptr);
@@ -274,6 +321,7 @@ int Solver::step(double dt, int nsteps)
         ic_live = false;
         t += dt;
         steps_done++;
+        probe_record();
     }
     return DG_OK;
 }
@@ -474,6 +522,8 @@ Solver::~Solver()
     if (d_bnd_ic) cudaFree(d_bnd_ic);
     if (d_bnd_ap) cudaFree(d_bnd_ap);
     if (d_bnd_src) cudaFree(d_bnd_src);
+    if (d_probe_off) cudaFree(d_probe_off);
+    if (d_probe_rec) cudaFree(d_probe_rec);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -574,6 +624,69 @@ int dg_get_grid(dg_handle* h, double* coords, double* sigma)
 double dg_time(const dg_handle* h) { return h ? h->s.t : 0.0; }
 
 long long dg_launch_count(const dg_handle* h) { return h ? h->s.launches : 0; }
+
+int dg_probe_set(dg_handle* h, int n, const double* xyz)
+{
+    if (!h || n < 0 || (n > 0 && !xyz)) return fail(DG_ERR_INVALID, "dg_probe_set: bad argument");
+    Solver& s = h->s;
+    cudaError_t e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    const dg::MeshHost& m = s.mesh;
+    const int K = m.K, K3 = K * K * K;
+    std::vector<long long> off(n);
+    std::vector<double> x;
+    for (int i = 0; i < n; i++) {
+        // the element containing the point (clamped to the mesh), then its nearest node
+        int g[3];
+        for (int a = 0; a < 3; a++) {
+            const double r = (xyz[3 * i + a] - s.p.corner[a]) / s.p.elem_width[a];
+            g[a] = std::min(m.E[a] - 1, std::max(0, (int)std::floor(r)));
+        }
+        const int el = m.elem_index(g);
+        m.node_coords(s.p, s.op, el, x);
+        int best = 0;
+        double bd = 1e300;
+        for (int nn = 0; nn < K3; nn++) {
+            double d2 = 0;
+            for (int a = 0; a < 3; a++) d2 += (x[a * K3 + nn] - xyz[3 * i + a]) * (x[a * K3 + nn] - xyz[3 * i + a]);
+            if (d2 < bd) {
+                bd = d2;
+                best = nn;
+            }
+        }
+        off[i] = (long long)el * m.NP + best;
+    }
+    if (s.d_probe_off) cudaFree(s.d_probe_off);
+    if (s.d_probe_rec) cudaFree(s.d_probe_rec);
+    s.d_probe_off = nullptr;
+    s.d_probe_rec = nullptr;
+    s.probe_cap = s.probe_steps = 0;
+    s.probe_t.clear();
+    s.n_probe = n;
+    if (n == 0) return DG_OK;
+    e = cudaMalloc(&s.d_probe_off, n * sizeof(long long));
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = cudaMemcpy(s.d_probe_off, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    return s.probe_reserve(1024);
+}
+
+int dg_probe_get(dg_handle* h, double* t, double* p, int max_steps, int* steps)
+{
+    if (!h || max_steps < 0) return fail(DG_ERR_INVALID, "dg_probe_get: bad argument");
+    Solver& s = h->s;
+    const long long ns = std::min<long long>(s.probe_steps, max_steps);
+    if (p && ns > 0 && s.n_probe > 0) {
+        cudaError_t e = cudaMemcpyAsync(p, s.d_probe_rec, (size_t)ns * s.n_probe * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("dg_probe_get: ") + cudaGetErrorString(e));
+    }
+    if (t)
+        for (long long i = 0; i < ns; i++) t[i] = s.probe_t[i];
+    if (steps) *steps = (int)s.probe_steps;
+    return DG_OK;
+}
 
 int dg_stream(dg_handle* h, void** stream)
 {

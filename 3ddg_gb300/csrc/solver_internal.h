@@ -47,6 +47,15 @@ struct Solver {
         long long launches = 0;
         double bytes = 0.0, flops = 0.0;
     };
+    // Pressure probes: node offsets (element * NP + node) and the record.
+    long long* d_probe_off = nullptr;
+    int n_probe = 0;
+    double* d_probe_rec = nullptr;  // [capacity][n_probe]
+    long long probe_cap = 0, probe_steps = 0;
+    std::vector<double> probe_t;
+    int probe_reserve(long long steps);
+    void probe_record();
+
     bool profiling = false;
     KernelStat kstat[2];
     std::vector<cudaEvent_t> event_pool;

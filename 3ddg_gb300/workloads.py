@@ -90,6 +90,56 @@ def config3(seed: int = 0) -> dict:
     return cfg
 
 
+FOCAL_PROBE_CONFIG1 = (0.0, 0.0, 2.5)  # on the pulse's z axis, 2.5 mm from its centre (mm)
+
+
+def harmonics(t: np.ndarray, p: np.ndarray):
+    """Fundamental frequency f1 (the largest non-zero DFT bin of the probe's
+    pressure record, Hann-windowed) and the amplitudes |P(f1)|, |P(2 f1)| (the
+    bin nearest to 2 f1).  Used as the focal-axis 2nd-harmonic measure."""
+    p = np.asarray(p, dtype=np.float64)
+    n = len(p)
+    w = np.hanning(n)
+    P = np.abs(np.fft.rfft(p * w)) * 2.0 / w.sum()
+    f = np.fft.rfftfreq(n, d=float(t[1] - t[0]) if n > 1 else 1.0)
+    k1 = 1 + int(np.argmax(P[1:]))
+    k2 = min(len(P) - 1, int(round(2 * k1)))
+    return float(f[k1]), float(P[k1]), float(P[k2])
+
+
+def config4(seed: int = 0, n: int = 256, steps: int = 500, width: float = 0.25) -> list:
+    """Batched form: n independent instances drawn from the seed.  Elements
+    per side uniform in 4..24 (each axis independently), N uniform in
+    {2, 3, 4, 5}, source amplitude log-uniform 0.1..5 MPa, centre frequency
+    uniform 0.5..2 MHz, sponge thickness 2..4 elements, sound speed
+    1.45..1.60 mm/us; FP32, ``steps`` RK steps each at CFL 0.5.  Each instance
+    is a single block of ``width``-mm elements, zero initial state, a 5-cycle
+    Hann tone burst on its z = 0 face (no sponge there) and sponges on the other
+    five faces."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n):
+        ne = [int(v) for v in rng.integers(4, 25, size=3)]
+        order = int(rng.integers(2, 6))
+        amp = float(np.exp(rng.uniform(np.log(0.1), np.log(5.0))))
+        freq = float(rng.uniform(0.5, 2.0))
+        sponge = int(rng.integers(2, 5))
+        c0 = float(rng.uniform(1.45, 1.60))
+        cfg = dict(
+            ORDER=order, NUM_ELEMENTS=ne, NUM_BLOCKS=[1, 1, 1], ELEMENT_WIDTH=[width] * 3,
+            STARTING_CORNER=[-0.5 * ne[0] * width, -0.5 * ne[1] * width, 0.0], EVALUATE_ADVECTION=1,
+            EVALUATE_DIFFUSION=1, EVALUATE_SPONGE=1, BC_IS_PERIODIC=[0, 0, 0], BC_SIGMA_MAX=0.5,
+            BC_SPONGE_WIDTH=[sponge, sponge, sponge, sponge, 0, sponge], IC_X_GAUSS=0, IC_Y_GAUSS=0,
+            IC_Z_GAUSS=0, IC_DRHO_AMPLITUDE=0.0, IC_VX_AMPLITUDE=0.0, IC_VY_AMPLITUDE=0.0,
+            IC_VZ_AMPLITUDE=0.0, IC_SIGMA=0.5, IC_CENTER_X=0.0, IC_CENTER_Y=0.0, IC_CENTER_Z=0.0,
+            SRC_FACE=4, SRC_AMPLITUDE=amp, SRC_FREQUENCY=freq, SRC_CYCLES=5.0, SRC_PHASE=0.0, SRC_RADIUS=0.0,
+            PRECISION=32, C0=c0, RHO0=WATER["RHO0"], B_OVER_A=WATER["B_OVER_A"], DIFF_CONST=WATER["DIFF_CONST"])
+        cfg["DT"] = cfl_dt(cfg)
+        cfg["STEPS"] = steps
+        out.append(cfg)
+    return out
+
+
 def scaled(cfg: dict, num_elements, num_blocks=(1, 1, 1)) -> dict:
     """The same physics on a different element count (same element width,
     domain re-centred in x and y, the z origin kept)."""

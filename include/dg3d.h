@@ -176,6 +176,17 @@ int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int grid);
 int dg_hdf5_write(const char* path, const char* name, int ndim, const long long* dims,
                   const double* data, double time);
 
+/* Pressure probes (no counterpart in the reference; for focal-axis and
+ * harmonic analysis): after every subsequent RK step the pressure
+ * p = c0^2 (drho + B/A drho^2 / (2 rho0)) at the node nearest to each of the n
+ * points xyz[3*i..3*i+2] is recorded on the device.  Calling it again
+ * replaces the probes and clears the record. */
+int dg_probe_set(dg_handle* h, int n, const double* xyz);
+/* Copy the record: up to max_steps rows of n values (step-major) into p and
+ * the time after each recorded step into t (either may be NULL); *steps
+ * receives the number of recorded steps.  Synchronous. */
+int dg_probe_get(dg_handle* h, double* t, double* p, int max_steps, int* steps);
+
 /* Number of kernel launches issued by this handle since creation (profiling). */
 long long dg_launch_count(const dg_handle* h);
 
@@ -199,6 +210,63 @@ int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double
  * element-major: field f, element e, node n at base[f] + e*node_stride + n,
  * node n = (i*K + j)*K + k.  For zero-copy integration and benchmarking. */
 int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem);
+
+/* ------------------------------------------------------------------------
+ * Batched form (no counterpart in the reference, which runs one problem per
+ * process): n independent problems of uneven element counts and orders
+ * (ORDER 1..5), FP32 fields/fluxes/stages with the Kahan-compensated update,
+ * advanced together by one persistent kernel per RK stage under a captured
+ * CUDA graph.  Problem i takes its own dt[i] and stops after steps[i] steps;
+ * its exterior state is zero except the tone-burst source (whole face).
+ * Each problem's result is independent of its batch-mates (bitwise).
+ * ------------------------------------------------------------------------ */
+typedef struct dg_batch dg_batch;
+int dg_batch_create(int n, const dg_params* params, const double* dt, const int* steps,
+                    const char* matrix_file, const char* coeff_file, dg_batch** out);
+int dg_batch_destroy(dg_batch* b);
+/* Advance every active problem nsteps steps (asynchronous). */
+int dg_batch_step(dg_batch* b, int nsteps);
+int dg_batch_synchronize(dg_batch* b);
+/* State of problem i in the dg_get_state layout (synchronous). */
+int dg_batch_get_state(dg_batch* b, int i, double* drho, double* vel);
+/* Node-duplicated dims, completed steps and time of problem i. */
+int dg_batch_info(dg_batch* b, int i, int* dims3, long long* steps_done, double* time);
+long long dg_batch_total_nodes(const dg_batch* b);
+/* Choose the tile size of every order and the persistent grid by timing
+ * trial_steps real steps per candidate; the state is restored afterwards.
+ * A summary of the choice is written to report (may be NULL). */
+int dg_batch_autotune(dg_batch* b, int trial_steps, char* report, size_t report_len);
+int dg_batch_stream(dg_batch* b, void** stream);
+long long dg_batch_launch_count(const dg_batch* b);
+
+/* ------------------------------------------------------------------------
+ * Serving form (no counterpart in the reference): a request loop that admits
+ * solves by an HBM budget, keeps their state on the device and batches their
+ * RK steps with every other in-flight solve (continuous batching, the batched
+ * form's kernels).  Clock: seconds since dg_serve_create.
+ * ------------------------------------------------------------------------ */
+typedef struct dg_server dg_server;
+/* keep_results != 0: copy each finished solve's state back for dg_serve_result. */
+int dg_serve_create(size_t hbm_budget_bytes, int keep_results, dg_server** out);
+int dg_serve_destroy(dg_server* s);
+double dg_serve_clock(const dg_server* s);
+/* Queue a solve arriving at arrival_time (server clock; < 0: now).  Rejected
+ * with DG_ERR_NOMEM if it alone exceeds the budget. */
+int dg_serve_submit(dg_server* s, const dg_params* p, double dt, int steps, double arrival_time,
+                    long long* id);
+/* One loop iteration: admit arrived requests that fit, advance every in-flight
+ * solve one RK step, retire the finished ones. */
+int dg_serve_tick(dg_server* s, int* n_inflight);
+/* Run the loop in real time until every submitted request has finished. */
+int dg_serve_run(dg_server* s, double max_seconds);
+/* Arrival, admission and completion times of a request; its final state when
+ * the server keeps results (drho/vel may be NULL). */
+int dg_serve_result(dg_server* s, long long id, double* t_arrival, double* t_admit, double* t_done,
+                    double* drho, double* vel);
+/* Completed requests, p50/p99 latency (s), completed solves per second over
+ * the span from the first arrival to the last completion, mean in-flight count. */
+int dg_serve_stats(dg_server* s, int* completed, double* p50, double* p99, double* solves_per_s,
+                   double* mean_inflight);
 
 /* Last error message of this thread ("" if none). */
 const char* dg_last_error(void);

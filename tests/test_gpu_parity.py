@@ -141,6 +141,25 @@ def test_set_state_clears_ic_halo(solver_for, oracle_for):
     compare_state(cfg, s, o, STEP_TOL)
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_probe_records_pressure_at_nearest_node(precision, solver_for):
+    cfg = small(order=3)
+    cfg["PRECISION"] = precision
+    s = solver_for(cfg)
+    pts = np.array([[0.3, -0.2, 0.1], [100.0, 100.0, -100.0]])
+    s.probe_set(pts)
+    for _ in range(3):
+        s.step(cfg["DT"], 2)
+    t, p = s.probe_get()
+    assert p.shape == (6, 2) and np.all(np.diff(t) > 0) and abs(t[-1] - s.time) < 1e-15
+    r, _ = s.state()
+    c, _ = s.grid()
+    for k, x in enumerate(pts):
+        d2 = sum((c[a] - x[a]) ** 2 for a in range(3))
+        idx = np.unravel_index(np.argmin(d2), d2.shape)
+        assert abs(p[-1, k] - pressure(cfg, r[idx])) <= 1e-12 * max(1.0, abs(p[-1, k]))
+
+
 def test_fp32_form_within_tolerance(solver_for, oracle_for):
     """FP32 fields/fluxes/stages with the Kahan-compensated update against the
     FP64 oracle: relative L2 pressure error <= 1e-5."""

@@ -1,0 +1,72 @@
+"""Serving form (dg_serve_*): continuous batching of solves that arrive while
+others run, admitted by an HBM budget.  Every result is the same alone and in
+the mix (bitwise: a problem's arithmetic never depends on its batch-mates)."""
+import numpy as np
+import pytest
+
+from conftest import dg, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def requests(n=5, seed=21):
+    W = workloads()
+    cfgs = W.config4(seed=seed, n=n, steps=30)
+    rng = np.random.default_rng(seed)
+    for c in cfgs:
+        c["NUM_ELEMENTS"] = [min(v, 7) for v in c["NUM_ELEMENTS"]]
+        c["STEPS"] = int(rng.integers(10, 40))
+    return cfgs
+
+
+def alone(cfg):
+    with dg().Batch([cfg]) as b:
+        b.step(cfg["STEPS"])
+        return b.state(0)
+
+
+def test_results_same_alone_and_in_the_mix():
+    m = dg()
+    cfgs = requests()
+    with m.Server(hbm_budget_bytes=8 << 30, keep_results=True) as srv:
+        t0 = srv.clock
+        ids = [srv.submit(c, arrival_time=t0 + 0.002 * k) for k, c in enumerate(cfgs)]
+        srv.run(max_seconds=120)
+        res = [srv.result(i, state=True) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(cfgs)
+    assert st["mean_inflight"] > 1.0  # requests overlapped on the device
+    for c, r in zip(cfgs, res):
+        assert r["done"] >= r["admit"] >= r["arrival"]
+        ra, va = alone(c)
+        assert np.array_equal(r["rho"], ra) and np.array_equal(r["vel"], va)
+
+
+def test_admission_respects_the_hbm_budget():
+    m = dg()
+    import importlib
+    cfgs = requests(n=6, seed=5)
+    for c in cfgs:
+        c["NUM_ELEMENTS"] = [6, 6, 6]
+        c["ORDER"] = 3
+        c["STEPS"] = 15
+    per = 216 * 64 * 23 * 4 + 216 * 28
+    with m.Server(hbm_budget_bytes=2 * per + 100) as srv:
+        for c in cfgs:
+            srv.submit(c, arrival_time=0.0)
+        peak = 0
+        while True:
+            n = srv.tick()
+            peak = max(peak, n)
+            if all(srv.result(i + 1)["done"] >= 0 for i in range(len(cfgs))):
+                break
+        st = srv.stats()
+    assert peak == 2 and st["completed"] == 6
+
+
+def test_request_larger_than_budget_rejected():
+    m = dg()
+    c = requests(n=1)[0]
+    with m.Server(hbm_budget_bytes=1 << 20) as srv:
+        with pytest.raises(m.DGError, match="more than the whole HBM budget"):
+            srv.submit(c)
