@@ -162,17 +162,40 @@ __device__ __forceinline__ int axis_stride(int a)
 // M^-1 e_N F_N) with the central flux F_0 = (drho_o[N] + drho_s[0]) / 2,
 // F_N = -(drho_s[N] + drho_o[0]) / 2.
 // ---------------------------------------------------------------------------
+// Each thread's rows of the per-launch operator (its index along each axis),
+// loaded once through L1 into registers.  The operator lives in global memory:
+// indexing kernel-parameter space with a per-thread index would serialise on
+// the address-divergence unit.
+template <typename T, int K>
+struct OpRows {
+    T d[3][K], l0[3], ln[3];
+    __device__ __forceinline__ void load(const OpConst<T, K>& C, const int c[3], bool act)
+    {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int ia = act ? c[a] : 0;
+            l0[a] = C.L0[ia];
+            ln[a] = C.LN[ia];
+#pragma unroll
+            for (int j = 0; j < K; j++) d[a][j] = C.D[a][ia][j];
+        }
+    }
+};
+
 template <typename T, int K, bool INCR>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
-ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C)
+ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp)
 {
     constexpr int K2 = K * K, K3 = K * K * K;
     __shared__ GradSmem<T, K> sm_all[epb_of(K)];
     GradSmem<T, K>& S = sm_all[threadIdx.y];
+    const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
     const int e = blockIdx.x * epb_of(K) + threadIdx.y;
     const bool act = n < K3 && e < m.n_elem;
     const int c[3] = {n / K2, (n / K) % K, n % K};
+    OpRows<T, K> R;
+    R.load(C, c, act);
     T rho = T(0);
     if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
     S.r[n] = rho;
@@ -201,11 +224,12 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C)
         const int ia = c[a];
         const int base = n - ia * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T s = C.L0[ia] * S.fl[a][0][fi];
-        s += C.LN[ia] * S.fl[a][1][fi];
+        T s = R.l0[a] * S.fl[a][0][fi];
+        s += R.ln[a] * S.fl[a][1][fi];
 #pragma unroll
-        for (int j = 0; j < K; j++) s += C.D[a][ia][j] * S.r[base + j * st];
+        for (int j = 0; j < K; j++) s += R.d[a][j] * S.r[base + j * st];
         io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
+        (void)ia;
     }
 }
 
@@ -214,16 +238,19 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C)
 // ---------------------------------------------------------------------------
 template <typename T, int K, bool DIFF, bool INCR>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
-stage_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C, int do_adv, int do_sponge)
+stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
     constexpr int K2 = K * K, K3 = K * K * K;
     __shared__ StageSmem<T, K> sm_all[epb_of(K)];
     StageSmem<T, K>& S = sm_all[threadIdx.y];
+    const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
     const int e = blockIdx.x * epb_of(K) + threadIdx.y;
     const bool act = n < K3 && e < m.n_elem;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const size_t off = (size_t)e * io.np + n;
+    OpRows<T, K> R;
+    R.load(C, c, act);
 
     T rho = T(0), u[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     if (act) {
@@ -286,18 +313,19 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, OpConst<T, K> C, int do_adv, int do_sp
     for (int a = 0; a < 3; a++) {
         const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T sr = C.L0[ia] * S.gr[a][0][fi];
-        sr += C.LN[ia] * S.gr[a][1][fi];
+        T sr = R.l0[a] * S.gr[a][0][fi];
+        sr += R.ln[a] * S.gr[a][1][fi];
 #pragma unroll
-        for (int j = 0; j < K; j++) sr += C.D[a][ia][j] * S.fh[a][base + j * st];
+        for (int j = 0; j < K; j++) sr += R.d[a][j] * S.fh[a][base + j * st];
         r_rho += sr;
         if (do_adv) {
-            T sm = C.L0[ia] * S.gm[a][0][fi];
-            sm += C.LN[ia] * S.gm[a][1][fi];
+            T sm = R.l0[a] * S.gm[a][0][fi];
+            sm += R.ln[a] * S.gm[a][1][fi];
 #pragma unroll
-            for (int j = 0; j < K; j++) sm += C.D[a][ia][j] * S.fm[base + j * st];
+            for (int j = 0; j < K; j++) sm += R.d[a][j] * S.fm[base + j * st];
             r_u[a] = sm;
         }
+        (void)ia;
     }
     const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);
 
@@ -424,6 +452,47 @@ __device__ __forceinline__ size_t grid_index(const GridMap& g, int e, int n)
     const size_t jj = (size_t)(b1 * g.ne[1] + l1) * K + (n / K) % K;
     const size_t kk = (size_t)(b2 * g.ne[2] + l2) * K + n % K;
     return (ii * ((size_t)g.E[1] * K) + jj) * ((size_t)g.E[2] * K) + kk;
+}
+
+// Element-major offset (e * NP + n) of the node at node-duplicated position
+// (ii, jj, kk): the inverse of grid_index.
+__device__ __forceinline__ size_t elem_offset(const GridMap& g, int np, size_t ii, size_t jj, size_t kk)
+{
+    const int K = g.K;
+    const int gx = (int)(ii / K), gy = (int)(jj / K), gz = (int)(kk / K);
+    const int a = (int)(ii % K), b = (int)(jj % K), c = (int)(kk % K);
+    const int bx = gx / g.ne[0], by = gy / g.ne[1], bz = gz / g.ne[2];
+    const int lx = gx % g.ne[0], ly = gy % g.ne[1], lz = gz % g.ne[2];
+    const size_t e = (size_t)((bx * g.nb[1] + by) * g.nb[2] + bz) * g.elem_per_block + (lx * g.ne[1] + ly) * g.ne[2] + lz;
+    return e * np + (a * K + b) * K + c;
+}
+
+// State <-> host-order arrays rho [X][Y][Z], vel [3][X][Y][Z], walked in host
+// order so that rho/vel may be pinned host memory read or written directly by
+// the kernel (streaming, coalesced on the host side), or device staging.
+template <typename T>
+__global__ void pack_host_order_kernel(const T* __restrict__ state, size_t fs, int np, GridMap g,
+                                       double* __restrict__ rho, double* __restrict__ vel, size_t gsize)
+{
+    const size_t Y = (size_t)g.E[1] * g.K, Z = (size_t)g.E[2] * g.K;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < gsize; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t o = elem_offset(g, np, i / (Y * Z), (i / Z) % Y, i % Z);
+        if (rho) rho[i] = (double)state[o];
+        if (vel)
+            for (int a = 0; a < 3; a++) vel[a * gsize + i] = (double)state[(size_t)(1 + a) * fs + o];
+    }
+}
+
+template <typename T>
+__global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g,
+                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize)
+{
+    const size_t Y = (size_t)g.E[1] * g.K, Z = (size_t)g.E[2] * g.K;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < gsize; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t o = elem_offset(g, np, i / (Y * Z), (i / Z) % Y, i % Z);
+        state[o] = (T)rho[i];
+        for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + o] = (T)vel[a * gsize + i];
+    }
 }
 
 template <typename T>

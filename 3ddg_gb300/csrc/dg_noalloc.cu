@@ -36,10 +36,12 @@ constexpr size_t kMaxSlots = DG_NOALLOC_MAX_NODES;    // n_elem * NP, padded nod
 constexpr size_t kMaxElems = DG_NOALLOC_MAX_ELEMENTS;
 constexpr size_t kQBytes = 3 * kMaxSlots * sizeof(double);
 constexpr size_t kFlagBytes = 6 * kMaxElems * sizeof(int);
+constexpr size_t kConstSlot = 4096;  // one per-launch operator (OpConst<double, 8> fits)
 
-// LDG gradient (3 x kMaxSlots doubles) followed by the boundary-source flags
-// (6 x kMaxElems ints, zero: every boundary face reads a zero exterior state).
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kQBytes + kFlagBytes];
+// LDG gradient (3 x kMaxSlots doubles), the boundary-source flags (6 x
+// kMaxElems ints, zero: every boundary face reads a zero exterior state) and
+// two operator slots (stage, gradient).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kQBytes + kFlagBytes + 2 * kConstSlot];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
@@ -105,21 +107,30 @@ bool line_operators_stack(int K, const double* M, const double* S, double* D, do
 }
 
 template <int K>
-void launch(const dg_params& p, const double* D, const double* L0, const double* LN, const dg::StageIO<double>& io,
-            const dg::MeshDev<double>& md, cudaStream_t st)
+cudaError_t launch(const dg_params& p, const double* D, const double* L0, const double* LN,
+                   const dg::StageIO<double>& io, const dg::MeshDev<double>& md, unsigned char* consts,
+                   cudaStream_t st)
 {
+    static_assert(sizeof(dg::OpConst<double, K>) <= kConstSlot, "operator slot too small");
     const dg::OpConst<double, K> C = dg::make_stage_const<double, K>(1.0, D, L0, LN, p.elem_width, p.rho0, p.c0,
                                                                      p.b_over_a, p.diff_const);
+    const dg::OpConst<double, K> G =
+        dg::make_grad_const<double, K>(D, L0, LN, p.elem_width, p.rho0, p.c0, p.diff_const);
+    // stream-ordered copies from the stack (staged by the runtime before return)
+    cudaError_t e = cudaMemcpyAsync(consts, &C, sizeof C, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(consts + kConstSlot, &G, sizeof G, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    const dg::OpConst<double, K>* Cd = (const dg::OpConst<double, K>*)consts;
+    const dg::OpConst<double, K>* Gd = (const dg::OpConst<double, K>*)(consts + kConstSlot);
     dim3 block(dg::npt_of(K), dg::epb_of(K));
     dim3 grid((md.n_elem + dg::epb_of(K) - 1) / dg::epb_of(K));
     if (p.eval_diff) {
-        const dg::OpConst<double, K> G =
-            dg::make_grad_const<double, K>(D, L0, LN, p.elem_width, p.rho0, p.c0, p.diff_const);
-        dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, G);
-        dg::stage_kernel<double, K, true, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
+        dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, Gd);
+        dg::stage_kernel<double, K, true, false><<<grid, block, 0, st>>>(io, md, Cd, p.eval_advect, p.eval_sponge);
     } else {
-        dg::stage_kernel<double, K, false, false><<<grid, block, 0, st>>>(io, md, C, p.eval_advect, p.eval_sponge);
+        dg::stage_kernel<double, K, false, false><<<grid, block, 0, st>>>(io, md, Cd, p.eval_advect, p.eval_sponge);
     }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -152,6 +163,7 @@ extern "C" int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const
     cudaStream_t st = (cudaStream_t)stream;
     double* q = (double*)scratch;
     int* flags = (int*)((unsigned char*)scratch + kQBytes);
+    unsigned char* consts = (unsigned char*)scratch + kQBytes + kFlagBytes;
     cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)6 * n_elem * sizeof(int), st);
     if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
 
@@ -175,15 +187,15 @@ extern "C" int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const
     md.ic_live = 0;
     md.src_p = 0.0;
     switch (K) {
-    case 2: launch<2>(*p, D, L0, LN, io, md, st); break;
-    case 3: launch<3>(*p, D, L0, LN, io, md, st); break;
-    case 4: launch<4>(*p, D, L0, LN, io, md, st); break;
-    case 5: launch<5>(*p, D, L0, LN, io, md, st); break;
-    case 6: launch<6>(*p, D, L0, LN, io, md, st); break;
-    case 7: launch<7>(*p, D, L0, LN, io, md, st); break;
-    case 8: launch<8>(*p, D, L0, LN, io, md, st); break;
+    case 2: e = launch<2>(*p, D, L0, LN, io, md, consts, st); break;
+    case 3: e = launch<3>(*p, D, L0, LN, io, md, consts, st); break;
+    case 4: e = launch<4>(*p, D, L0, LN, io, md, consts, st); break;
+    case 5: e = launch<5>(*p, D, L0, LN, io, md, consts, st); break;
+    case 6: e = launch<6>(*p, D, L0, LN, io, md, consts, st); break;
+    case 7: e = launch<7>(*p, D, L0, LN, io, md, consts, st); break;
+    case 8: e = launch<8>(*p, D, L0, LN, io, md, consts, st); break;
     }
-    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return DG_OK;
 }

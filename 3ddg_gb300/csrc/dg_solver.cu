@@ -85,35 +85,87 @@ double stage_flops(const Solver& s, bool has_old)
     return f * (double)s.gsize();
 }
 
+// Per-launch operators live in a small device buffer (one slot each for the
+// three RK stages, the LDG gradient and a bare right-hand side), rebuilt
+// only when dt changes.
+template <typename T, int K>
+size_t const_slot()
+{
+    return (sizeof(OpConst<T, K>) + 255) / 256 * 256;
+}
+
+template <typename T, int K>
+int upload_consts_k(Solver& s, double dt)
+{
+    const size_t slot = const_slot<T, K>();
+    std::vector<char> h(5 * slot, 0);
+    const double cas[5] = {dt, dt * .25, dt * 2.0 / 3.0, 0.0, 1.0};
+    for (int i = 0; i < 5; i++) {
+        const OpConst<T, K> C =
+            i == 3 ? make_grad_const<T, K>(s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(), s.p.elem_width,
+                                           s.p.rho0, s.p.c0, s.p.diff_const)
+                   : make_stage_const<T, K>(cas[i], s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(),
+                                            s.p.elem_width, s.p.rho0, s.p.c0, s.p.b_over_a, s.p.diff_const);
+        std::memcpy(h.data() + i * slot, &C, sizeof C);
+    }
+    if (!s.d_const) {
+        cudaError_t e = cudaMalloc(&s.d_const, 5 * slot);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    // stream-ordered after every launch that used the previous operators
+    cudaError_t e = cudaMemcpyAsync(s.d_const, h.data(), 5 * slot, cudaMemcpyHostToDevice, s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    s.const_dt = dt;
+    return DG_OK;
+}
+
+template <typename T, int K>
+const OpConst<T, K>* const_ptr(const Solver& s, int slot)
+{
+    return (const OpConst<T, K>*)((const char*)s.d_const + (size_t)slot * const_slot<T, K>());
+}
+
 template <typename T, int K, bool INCR>
 void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 {
-    const OpConst<T, K> C = make_grad_const<T, K>(s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(),
-                                                  s.p.elem_width, s.p.rho0, s.p.c0, s.p.diff_const);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(1, &ev);
-    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, C);
+    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, const_ptr<T, K>(s, 3));
     s.prof_end(1, ev, grad_bytes(s, io), grad_flops(s));
     s.launches++;
 }
 
 template <typename T, int K, bool INCR>
-void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, double ca)
+void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slot)
 {
-    const OpConst<T, K> C = make_stage_const<T, K>(ca, s.op.deriv.data(), s.op.lift0.data(), s.op.liftN.data(),
-                                                   s.p.elem_width, s.p.rho0, s.p.c0, s.p.b_over_a, s.p.diff_const);
+    const OpConst<T, K>* Cp = const_ptr<T, K>(s, slot);
     dim3 block(npt_of(K), epb_of(K));
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(0, &ev);
     if (s.p.eval_diff)
-        stage_kernel<T, K, true, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
+        stage_kernel<T, K, true, INCR><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
     else
-        stage_kernel<T, K, false, INCR><<<grid, block, 0, s.stream>>>(io, md, C, s.p.eval_advect, s.p.eval_sponge);
+        stage_kernel<T, K, false, INCR><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
     s.prof_end(0, ev, stage_bytes<T, INCR>(s, io), stage_flops(s, io.old != nullptr || io.inc != nullptr));
     s.launches++;
+}
+
+template <typename T>
+int upload_consts(Solver& s, double dt)
+{
+    switch (s.mesh.K) {
+    case 2: return upload_consts_k<T, 2>(s, dt);
+    case 3: return upload_consts_k<T, 3>(s, dt);
+    case 4: return upload_consts_k<T, 4>(s, dt);
+    case 5: return upload_consts_k<T, 5>(s, dt);
+    case 6: return upload_consts_k<T, 6>(s, dt);
+    case 7: return upload_consts_k<T, 7>(s, dt);
+    case 8: return upload_consts_k<T, 8>(s, dt);
+    }
+    return fail(DG_ERR_INVALID, "unsupported order");
 }
 
 template <typename T, bool INCR>
@@ -131,16 +183,16 @@ void dispatch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 }
 
 template <typename T, bool INCR>
-void dispatch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, double ca)
+void dispatch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slot)
 {
     switch (s.mesh.K) {
-    case 2: launch_stage<T, 2, INCR>(s, io, md, ca); break;
-    case 3: launch_stage<T, 3, INCR>(s, io, md, ca); break;
-    case 4: launch_stage<T, 4, INCR>(s, io, md, ca); break;
-    case 5: launch_stage<T, 5, INCR>(s, io, md, ca); break;
-    case 6: launch_stage<T, 6, INCR>(s, io, md, ca); break;
-    case 7: launch_stage<T, 7, INCR>(s, io, md, ca); break;
-    case 8: launch_stage<T, 8, INCR>(s, io, md, ca); break;
+    case 2: launch_stage<T, 2, INCR>(s, io, md, slot); break;
+    case 3: launch_stage<T, 3, INCR>(s, io, md, slot); break;
+    case 4: launch_stage<T, 4, INCR>(s, io, md, slot); break;
+    case 5: launch_stage<T, 5, INCR>(s, io, md, slot); break;
+    case 6: launch_stage<T, 6, INCR>(s, io, md, slot); break;
+    case 7: launch_stage<T, 7, INCR>(s, io, md, slot); break;
+    case 8: launch_stage<T, 8, INCR>(s, io, md, slot); break;
     }
 }
 
@@ -216,8 +268,12 @@ int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
     }
     md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
     md.src_p = burst_pressure(p, tst[s_idx]);
+    if (!d_const || (!rhs_only && dt != const_dt)) {
+        int rc = upload_consts<double>(*this, dt);
+        if (rc) return rc;
+    }
     if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
-    dispatch_stage<double, false>(*this, io, md, io.ca);
+    dispatch_stage<double, false>(*this, io, md, rhs_only ? 4 : s_idx);
     return DG_OK;
 }
 
@@ -257,8 +313,13 @@ int Solver::rk_stage_fp32(int s_idx, double dt, float* rhs_only)
     }
     md.ic_live = (s_idx == 0 && ic_live) ? 1 : 0;
     md.src_p = (float)burst_pressure(p, tst[s_idx]);
+    if (!d_const || (!rhs_only && dt != const_dt)) {
+        int rc = upload_consts<float>(*this, dt);
+        if (rc) return rc;
+    }
+    (void)ca;
     if (p.eval_diff) dispatch_grad<float, true>(*this, io, md);
-    dispatch_stage<float, true>(*this, io, md, ca);
+    dispatch_stage<float, true>(*this, io, md, rhs_only ? 4 : s_idx);
     return DG_OK;
 }
 
@@ -344,45 +405,77 @@ int Solver::ensure_staging()
     return DG_OK;
 }
 
+namespace {
+
+// Device address of pinned (page-locked, mapped) host memory, or null when the
+// pointer is ordinary pageable memory that a kernel must not touch.
+const void* device_view(const void* host)
+{
+    if (!host) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
+}  // namespace
+
+// Host transfers.  Pinned host buffers are read/written directly by the
+// host-order kernels over the CPU-GPU link (no staging copy); pageable ones go
+// through the device staging buffer and bulk copies.
 int Solver::pack_out(const void* src, double* drho, double* vel)
 {
-    int rc = ensure_staging();
-    if (rc) return rc;
     const GridMap g = grid_map(mesh);
-    const int threads = 256;
-    const long long total = (long long)mesh.n_elem * mesh.K * mesh.K * mesh.K;
-    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 152LL * 32);
+    const int threads = 256, blocks = 152 * 16;
+    double* rho_d = (double*)device_view(drho);
+    double* vel_d = (double*)device_view(vel);
+    const bool direct = (!drho || rho_d) && (!vel || vel_d);
+    if (!direct) {
+        int rc = ensure_staging();
+        if (rc) return rc;
+        rho_d = drho ? staging : nullptr;
+        vel_d = vel ? staging + gsize() : nullptr;
+    }
     if (fp64())
-        pack_grid_kernel<double><<<blocks, threads, 0, stream>>>((const double*)src, mesh.fstride(), mesh.NP, 4, g,
-                                                                 mesh.n_elem, staging, gsize());
+        pack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((const double*)src, mesh.fstride(), mesh.NP, g,
+                                                                       rho_d, vel_d, gsize());
     else
-        pack_grid_kernel<float><<<blocks, threads, 0, stream>>>((const float*)src, mesh.fstride(), mesh.NP, 4, g,
-                                                                mesh.n_elem, staging, gsize());
+        pack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((const float*)src, mesh.fstride(), mesh.NP, g,
+                                                                      rho_d, vel_d, gsize());
     launches++;
     DG_CUDA(cudaGetLastError());
-    if (drho) DG_CUDA(cudaMemcpyAsync(drho, staging, gsize() * sizeof(double), cudaMemcpyDeviceToHost, stream));
-    if (vel)
-        DG_CUDA(cudaMemcpyAsync(vel, staging + gsize(), 3 * gsize() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (!direct) {
+        if (drho) DG_CUDA(cudaMemcpyAsync(drho, staging, gsize() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        if (vel)
+            DG_CUDA(cudaMemcpyAsync(vel, staging + gsize(), 3 * gsize() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    stream));
+    }
     DG_CUDA(cudaStreamSynchronize(stream));
     return DG_OK;
 }
 
 int Solver::unpack_in(const double* drho, const double* vel)
 {
-    int rc = ensure_staging();
-    if (rc) return rc;
-    DG_CUDA(cudaMemcpyAsync(staging, drho, gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    DG_CUDA(cudaMemcpyAsync(staging + gsize(), vel, 3 * gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
     const GridMap g = grid_map(mesh);
-    const int threads = 256;
-    const long long total = (long long)mesh.n_elem * mesh.K * mesh.K * mesh.K;
-    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 152LL * 32);
+    const int threads = 256, blocks = 152 * 16;
+    const double* rho_d = (const double*)device_view(drho);
+    const double* vel_d = (const double*)device_view(vel);
+    if (!rho_d || !vel_d) {
+        int rc = ensure_staging();
+        if (rc) return rc;
+        DG_CUDA(cudaMemcpyAsync(staging, drho, gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        DG_CUDA(cudaMemcpyAsync(staging + gsize(), vel, 3 * gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        rho_d = staging;
+        vel_d = staging + gsize();
+    }
     if (fp64())
-        unpack_grid_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(), mesh.NP, 4,
-                                                                   g, mesh.n_elem, staging, gsize());
+        unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
+                                                                         mesh.NP, g, rho_d, vel_d, gsize());
     else {
-        unpack_grid_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP, 4, g,
-                                                                  mesh.n_elem, staging, gsize());
+        unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
+                                                                        g, rho_d, vel_d, gsize());
         DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
     }
     launches++;
@@ -522,6 +615,7 @@ Solver::~Solver()
     if (d_bnd_ic) cudaFree(d_bnd_ic);
     if (d_bnd_ap) cudaFree(d_bnd_ap);
     if (d_bnd_src) cudaFree(d_bnd_src);
+    if (d_const) cudaFree(d_const);
     if (d_probe_off) cudaFree(d_probe_off);
     if (d_probe_rec) cudaFree(d_probe_rec);
     if (stream) cudaStreamDestroy(stream);

@@ -35,6 +35,8 @@ struct Solver {
     void* d_bnd_ic = nullptr;
     void* d_bnd_ap = nullptr;
     int* d_bnd_src = nullptr;
+    void* d_const = nullptr;  // per-launch operators: 3 RK stages, LDG gradient, bare RHS
+    double const_dt = 0.0;
     int cur = 0;
     bool ic_live = false;
     double t = 0.0;

@@ -142,6 +142,28 @@ def test_set_state_clears_ic_halo(solver_for, oracle_for):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
+def test_pinned_host_buffers_match_pageable(precision, solver_for):
+    """Pinned host buffers are read/written by the kernels directly; pageable
+    ones go through device staging.  Both give the same bytes."""
+    import torch
+    cfg = small(order=3, ne=(3, 4, 2))
+    cfg["PRECISION"] = precision
+    s = solver_for(cfg)
+    s.step(cfg["DT"], 3)
+    r, v = s.state()
+    rp = torch.empty(r.shape, dtype=torch.float64, pin_memory=True).numpy()
+    vp = torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy()
+    s.state(rp, vp)
+    assert np.array_equal(r, rp) and np.array_equal(v, vp)
+    rp[...] = r * 1.5
+    vp[...] = v * 0.5
+    s.set_state(rp, vp)
+    r2, v2 = s.state()
+    tol = 0 if precision == 64 else 1e-6
+    assert np.allclose(r2, rp, rtol=tol, atol=0) and np.allclose(v2, vp, rtol=tol, atol=0)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
 def test_probe_records_pressure_at_nearest_node(precision, solver_for):
     cfg = small(order=3)
     cfg["PRECISION"] = precision
