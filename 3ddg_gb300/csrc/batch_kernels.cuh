@@ -126,9 +126,8 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
 #pragma unroll
         for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, P.r0, P.linear_mass);
         if (slot < EPB) {
-            S.fm[n] = fmom;
 #pragma unroll
-            for (int a = 0; a < 3; a++) S.fh[a][n] = fmass[a] + q[a];
+            for (int a = 0; a < 3; a++) S.f[a][n] = make_float2(fmom, fmass[a] + q[a]);
         }
         if (act) {
 #pragma unroll
@@ -151,9 +150,9 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
                 const float fao = mass_flux(uo, ro, P.r0, P.linear_mass);
                 const float* cm = P.cM[side];
                 const float* cr = P.cA[side];
-                S.gm[a][side][fi] = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
-                S.gr[a][side][fi] = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3] +
-                                    (side ? -0.5f : 0.5f) * (qo + q[a]);
+                S.g[a][side][fi] = make_float2(fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3],
+                                               fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3] +
+                                                   (side ? -0.5f : 0.5f) * (qo + q[a]));
             }
         }
         __syncthreads();
@@ -163,15 +162,16 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
             for (int a = 0; a < 3; a++) {
                 const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
                 const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                float sr = P.L0[ia] * S.gr[a][0][fi];
-                sr += P.LN[ia] * S.gr[a][1][fi];
-                float sm = P.L0[ia] * S.gm[a][0][fi];
-                sm += P.LN[ia] * S.gm[a][1][fi];
+                const float2 g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
+                float sm = P.L0[ia] * g0.x, sr = P.L0[ia] * g0.y;
+                sm += P.LN[ia] * gN.x;
+                sr += P.LN[ia] * gN.y;
 #pragma unroll
                 for (int j = 0; j < K; j++) {
                     const float dj = P.D[ia][j];
-                    sr += dj * S.fh[a][base + j * st];
-                    sm += dj * S.fm[base + j * st];
+                    const float2 v = S.f[a][base + j * st];
+                    sm += dj * v.x;
+                    sr += dj * v.y;
                 }
                 r_rho += P.invw[a] * sr;
                 r_u[a] = P.invw[a] * sm;

@@ -110,12 +110,24 @@ __device__ __forceinline__ T mass_flux(T u, T d, const T r0, int linear)
     return linear ? u * r0 : u * (d + r0);
 }
 
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+    using type = float2;
+};
+template <>
+struct Pair<double> {
+    using type = double2;
+};
+
+// Per element: for each axis a, the pair (f_mom, f_mass along a + G_a) of every
+// node, and the pair (momentum, density) of every face term, so each step of a
+// line sum is one 8- or 16-byte shared-memory load feeding two FMAs.
 template <typename T, int K>
 struct StageSmem {
-    T fm[npt_of(K)];       // momentum flux f_mom
-    T fh[3][npt_of(K)];    // f_mass along axis a plus the LDG gradient along a
-    T gm[3][2][K * K];     // momentum face terms [axis][side][face node]
-    T gr[3][2][K * K];     // density face terms (mass + diffusion)
+    typename Pair<T>::type f[3][npt_of(K)];
+    typename Pair<T>::type g[3][2][K * K];  // [axis][side][face node]
 };
 
 template <typename T, int K>
@@ -236,8 +248,20 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 // ---------------------------------------------------------------------------
 // One RK stage: R = L(stage input), then the stage combination.
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM asked of the compiler (0: no request).  The FP32 stage
+// kernel waits on global loads (long-scoreboard stalls), so where the
+// compiler can fit it in fewer registers without spilling it trades them for
+// resident warps: 40 registers at K = 2, 48 at K = 5 (the common N = 4).  The
+// FP64 kernel is bound by the FP64 pipe and keeps its registers.
+template <typename T, int K>
+__host__ __device__ constexpr int stage_min_blocks()
+{
+    return sizeof(T) != 4 ? 0 : (K == 2 ? 65536 / (40 * npt_of(K) * epb_of(K))
+                                        : (K == 5 ? 65536 / (48 * npt_of(K) * epb_of(K)) : 0));
+}
+
 template <typename T, int K, bool DIFF, bool INCR>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (stage_min_blocks<T, K>()))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
     constexpr int K2 = K * K, K3 = K * K * K;
@@ -267,9 +291,11 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 #pragma unroll
         for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, C.r0, C.linear_mass);
     }
-    S.fm[n] = fmom;
 #pragma unroll
-    for (int a = 0; a < 3; a++) S.fh[a][n] = DIFF ? fmass[a] + q[a] : fmass[a];
+    for (int a = 0; a < 3; a++) {
+        S.f[a][n].x = fmom;
+        S.f[a][n].y = DIFF ? fmass[a] + q[a] : fmass[a];
+    }
 
     // Face terms: the thread owning a face node evaluates that face's numerical
     // flux for its line (impedance upwind for advection, central for LDG),
@@ -301,8 +327,8 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
                 gr = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3];
             }
             if (DIFF) gr += C.cQ[a][side] * (qo + q[a]);
-            S.gm[a][side][fi] = gm;
-            S.gr[a][side][fi] = gr;
+            S.g[a][side][fi].x = gm;
+            S.g[a][side][fi].y = gr;
         }
     }
     __syncthreads();
@@ -313,18 +339,18 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     for (int a = 0; a < 3; a++) {
         const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T sr = R.l0[a] * S.gr[a][0][fi];
-        sr += R.ln[a] * S.gr[a][1][fi];
+        const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
+        T sm = R.l0[a] * g0.x, sr = R.l0[a] * g0.y;
+        sm += R.ln[a] * gN.x;
+        sr += R.ln[a] * gN.y;
 #pragma unroll
-        for (int j = 0; j < K; j++) sr += R.d[a][j] * S.fh[a][base + j * st];
-        r_rho += sr;
-        if (do_adv) {
-            T sm = R.l0[a] * S.gm[a][0][fi];
-            sm += R.ln[a] * S.gm[a][1][fi];
-#pragma unroll
-            for (int j = 0; j < K; j++) sm += R.d[a][j] * S.fm[base + j * st];
-            r_u[a] = sm;
+        for (int j = 0; j < K; j++) {
+            const typename Pair<T>::type v = S.f[a][base + j * st];
+            sm += R.d[a][j] * v.x;
+            sr += R.d[a][j] * v.y;
         }
+        r_rho += sr;
+        r_u[a] = do_adv ? sm : T(0);
         (void)ia;
     }
     const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);

@@ -343,11 +343,19 @@ def run_ours(a, dist: Dist):
         return None
     peak, peak_kind = measured_peaks()
     kind = "fp64"
+    fp64 = cfg.get("PRECISION", 64) == 64
+    ctype = "double" if fp64 else "float"
+    ne_g = [cfg["NUM_ELEMENTS"][i] * cfg["NUM_BLOCKS"][i] for i in range(3)]
+    nb = cfg["NUM_BLOCKS"]
+    buf_gb = 4 * nodes * (8 if fp64 else 4) / 1e9
+    workload = ("%s: %dx%dx%d hex elements N=%d in %dx%dx%d blocks, %s, water, tone burst, adv+LDG diffusion+sponge"
+                % ("config2" if not a.elements else "config2 physics, resized", ne_g[0], ne_g[1], ne_g[2],
+                   cfg["ORDER"], nb[0], nb[1], nb[2], "FP64" if fp64 else "FP32"))
     ach = (st_b / st_n) / (st_ms / st_n / 1e3) / 1e9 if st_n else None
     traffic = profiled_traffic(kind)
     roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
             "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-            else "fallback 6.8 TB/s", "kernel": "stage_kernel<double,5,DIFF>",
+            else "fallback 6.8 TB/s", "kernel": "stage_kernel<%s,%d,DIFF>" % (ctype, cfg["ORDER"] + 1),
             "algorithmic_bytes_per_launch": st_b / st_n if st_n else None,
             "mean_launch_ms": st_ms / st_n if st_n else None,
             "fp64_pipe": {"achieved_tflops": (st_f / st_n) / (st_ms / st_n / 1e3) / 1e12 if st_n else None,
@@ -360,11 +368,11 @@ def run_ours(a, dist: Dist):
     line = {
         "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tone burst, no IC)",
-        "config": {"workload": "config2: 64x64x64 hex elements N=4 in 2x2x2 blocks, FP64, water, tone burst, "
-                               "adv+LDG diffusion+sponge", "nodes": nodes, "dofs": 4 * nodes,
+        "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic (seeded tone burst, no IC)",
+        "config": {"workload": workload, "nodes": nodes, "dofs": 4 * nodes,
                    "parallelism": "replicas" if dist.world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (state 1.05 GB per buffer)", "dt_us": dt},
+                   "l2": "inputs %s than L2 (state %.3g GB per buffer)" % ("larger" if buf_gb > 0.129 else "smaller",
+                                                                          buf_gb), "dt_us": dt},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": step_bytes, "d2h_bytes_per_step": step_bytes,
                 "steps": ne2e, "ms_per_step": e2e_ms / ne2e},
         "gpu_launches": launches,
