@@ -90,6 +90,9 @@ def lib():
             "dg_write_snapshot": (i, [vp, cp, i, i]),
             "dg_launch_count": (C.c_longlong, [vp]),
             "dg_hdf5_write": (i, [cp, cp, i, C.POINTER(C.c_longlong), vp, d]),
+            "dg_hdf5_read": (i, [cp, cp, i, C.POINTER(C.c_longlong), C.POINTER(i), vp, C.c_longlong,
+                                 C.POINTER(i)]),
+            "dg_read_snapshot": (i, [vp, cp, i]),
             "dg_probe_set": (i, [vp, i, vp]),
             "dg_probe_get": (i, [vp, vp, vp, i, C.POINTER(i)]),
             "dg_stream": (i, [vp, C.POINTER(vp)]),
@@ -298,6 +301,10 @@ class Solver:
     def write_snapshot(self, folder: str, ts: int, grid: bool = False):
         _check(lib().dg_write_snapshot(self.h, _b(folder), int(ts), int(grid)), "dg_write_snapshot")
 
+    def read_snapshot(self, folder: str, ts: int):
+        """Restart: state and time from the snapshot files of time step ts."""
+        _check(lib().dg_read_snapshot(self.h, _b(folder), int(ts)), "dg_read_snapshot")
+
     def device_state(self):
         base = (C.c_void_p * 4)()
         ns = C.c_size_t()
@@ -472,6 +479,26 @@ def hdf5_write(path: str, name: str, data, time: float = 0.0):
     a = np.ascontiguousarray(data, dtype=np.float64)
     dims = (C.c_longlong * a.ndim)(*a.shape)
     _check(lib().dg_hdf5_write(_b(path), name.encode(), a.ndim, dims, _ptr(a), float(time)), "dg_hdf5_write")
+
+
+def hdf5_read(path: str, name: str):
+    """(array, type_class) of dataset ``name`` in an HDF5 file (float64 array;
+    type_class 0 integer, 1 floating point).  Raises DGError whose ``code`` is
+    the reference's HDF5 failure class (-1 file, -2 dataset, -3 dataspace,
+    -4 datatype)."""
+    L = lib()
+    dims = (C.c_longlong * 32)()
+    nd, cls = C.c_int(0), C.c_int(-1)
+    rc = L.dg_hdf5_read(_b(path), name.encode(), 32, dims, C.byref(nd), None, 0, C.byref(cls))
+    if rc == 0:
+        shape = tuple(dims[i] for i in range(nd.value))
+        out = np.empty(shape, dtype=np.float64)
+        rc = L.dg_hdf5_read(_b(path), name.encode(), 0, None, None, _ptr(out), out.size, None)
+    if rc != 0:
+        err = DGError("dg_hdf5_read failed (%d): %s" % (rc, L.dg_last_error().decode()))
+        err.code = rc
+        raise err
+    return out, cls.value
 
 
 def write_basis_files(folder: str, kmax: int = 10, lumped: bool = False):

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <new>
 
 namespace dg {
 
@@ -261,6 +262,274 @@ int h5_write(const std::string& path, const std::vector<H5Dataset>& sets_in)
     }
     ok = (std::fclose(fp) == 0) && ok;
     return ok ? 0 : -1;
+}
+
+}  // namespace dg
+
+// ---------------------------------------------------------------------------
+// Reader.  Every field read is bounds-checked against the file; a malformed
+// file gives an error code, never an out-of-range access.
+// ---------------------------------------------------------------------------
+namespace dg {
+
+namespace {
+
+struct H5Error {
+    int code;
+    std::string msg;
+};
+
+struct Reader {
+    std::vector<uint8_t> b;
+    void need(uint64_t off, uint64_t n, int code, const char* what) const
+    {
+        if (off > b.size() || n > b.size() - off) throw H5Error{code, std::string("truncated ") + what};
+    }
+    uint64_t uN(uint64_t off, int n, int code, const char* what) const
+    {
+        need(off, (uint64_t)n, code, what);
+        uint64_t v = 0;
+        for (int i = n - 1; i >= 0; i--) v = (v << 8) | b[off + i];
+        return v;
+    }
+    uint64_t u64(uint64_t off, int code, const char* what) const { return uN(off, 8, code, what); }
+    uint32_t u32(uint64_t off, int code, const char* what) const { return (uint32_t)uN(off, 4, code, what); }
+    uint16_t u16(uint64_t off, int code, const char* what) const { return (uint16_t)uN(off, 2, code, what); }
+    uint8_t u8(uint64_t off, int code, const char* what) const { return (uint8_t)uN(off, 1, code, what); }
+};
+
+struct MsgRef {
+    uint16_t type;
+    uint64_t off, size;
+};
+
+// Messages of a version-1 object header, following continuation messages.
+std::vector<MsgRef> header_messages(const Reader& r, uint64_t base, uint64_t addr, int code)
+{
+    if (r.u8(base + addr, code, "object header") != 1)
+        throw H5Error{code, "object header version is not 1"};
+    const uint16_t nmsg = r.u16(base + addr + 2, code, "object header");
+    const uint32_t size = r.u32(base + addr + 8, code, "object header");
+    std::vector<std::pair<uint64_t, uint64_t>> blocks{{base + addr + 16, size}};
+    std::vector<MsgRef> out;
+    for (size_t bi = 0; bi < blocks.size() && out.size() < nmsg; bi++) {
+        if (bi > 64) throw H5Error{code, "too many object header continuation blocks"};
+        uint64_t p = blocks[bi].first;
+        const uint64_t end = p + blocks[bi].second;
+        r.need(blocks[bi].first, blocks[bi].second, code, "object header block");
+        while (p + 8 <= end && out.size() < nmsg) {
+            const uint16_t type = r.u16(p, code, "message");
+            const uint16_t msize = r.u16(p + 2, code, "message");
+            if (p + 8 + msize > end) throw H5Error{code, "message overruns its header block"};
+            out.push_back({type, p + 8, msize});
+            if (type == 0x0010) {
+                blocks.push_back({base + r.u64(p + 8, code, "continuation"), r.u64(p + 16, code, "continuation")});
+            }
+            p += 8 + msize;
+        }
+    }
+    return out;
+}
+
+void walk_group_btree(const Reader& r, uint64_t base, uint64_t node, uint64_t heap_data, int depth,
+                      std::vector<std::pair<std::string, uint64_t>>& out)
+{
+    if (depth > 32) throw H5Error{-1, "group B-tree too deep"};
+    r.need(base + node, 24, -1, "B-tree node");
+    if (std::memcmp(&r.b[base + node], "TREE", 4) != 0) throw H5Error{-1, "bad B-tree node signature"};
+    if (r.u8(base + node + 4, -1, "B-tree") != 0) throw H5Error{-1, "not a group B-tree"};
+    const int level = r.u8(base + node + 5, -1, "B-tree");
+    const int used = r.u16(base + node + 6, -1, "B-tree");
+    uint64_t p = base + node + 24 + 8;  // past key 0
+    for (int i = 0; i < used; i++, p += 16) {
+        const uint64_t child = r.u64(p, -1, "B-tree child");
+        if (level > 0) {
+            walk_group_btree(r, base, child, heap_data, depth + 1, out);
+            continue;
+        }
+        r.need(base + child, 8, -1, "symbol table node");
+        if (std::memcmp(&r.b[base + child], "SNOD", 4) != 0) throw H5Error{-1, "bad symbol table node signature"};
+        const int nsym = r.u16(base + child + 6, -1, "symbol table node");
+        for (int k = 0; k < nsym; k++) {
+            const uint64_t e = base + child + 8 + 40ull * k;
+            const uint64_t noff = r.u64(e, -1, "symbol entry");
+            const uint64_t oh = r.u64(e + 8, -1, "symbol entry");
+            uint64_t s = base + heap_data + noff, q = s;
+            while (true) {
+                if (r.u8(q, -1, "link name") == 0) break;
+                q++;
+            }
+            out.push_back({std::string((const char*)&r.b[s], q - s), oh});
+        }
+    }
+}
+
+double to_double(const uint8_t* p, int cls, int size, bool be, bool sgn)
+{
+    uint8_t t[8];
+    for (int i = 0; i < size; i++) t[i] = be ? p[size - 1 - i] : p[i];
+    if (cls == 1) {
+        if (size == 8) {
+            double d;
+            std::memcpy(&d, t, 8);
+            return d;
+        }
+        float f;
+        std::memcpy(&f, t, 4);
+        return (double)f;
+    }
+    uint64_t v = 0;
+    for (int i = size - 1; i >= 0; i--) v = (v << 8) | t[i];
+    if (sgn && size < 8 && (v >> (8 * size - 1)) & 1) v |= ~0ull << (8 * size);
+    return sgn ? (double)(int64_t)v : (double)v;
+}
+
+}  // namespace
+
+int h5_read(const std::string& path, const std::string& name, std::vector<uint64_t>& dims,
+            std::vector<double>& data, int* type_class, std::string* why)
+{
+    try {
+        Reader r;
+        {
+            FILE* fp = std::fopen(path.c_str(), "rb");
+            if (!fp) throw H5Error{-1, "cannot open " + path};
+            std::fseek(fp, 0, SEEK_END);
+            const long n = std::ftell(fp);
+            std::fseek(fp, 0, SEEK_SET);
+            if (n < 0) {
+                std::fclose(fp);
+                throw H5Error{-1, "cannot size " + path};
+            }
+            r.b.resize((size_t)n);
+            const bool ok = std::fread(r.b.data(), 1, r.b.size(), fp) == r.b.size();
+            std::fclose(fp);
+            if (!ok) throw H5Error{-1, "cannot read " + path};
+        }
+        // The superblock sits at 0, 512, 1024, 2048, ...
+        static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+        uint64_t sb = UNDEF;
+        for (uint64_t o = 0; o + 8 <= r.b.size(); o = o ? 2 * o : 512)
+            if (std::memcmp(&r.b[o], sig, 8) == 0) {
+                sb = o;
+                break;
+            }
+        if (sb == UNDEF) throw H5Error{-1, "not an HDF5 file"};
+        const int ver = r.u8(sb + 8, -1, "superblock");
+        if (ver > 1) throw H5Error{-1, "superblock version " + std::to_string(ver) + " is not supported"};
+        if (r.u8(sb + 13, -1, "superblock") != 8 || r.u8(sb + 14, -1, "superblock") != 8)
+            throw H5Error{-1, "only 8-byte offsets and lengths are supported"};
+        const uint64_t fields = sb + 24 + (ver == 1 ? 4 : 0);
+        const uint64_t base = r.u64(fields, -1, "superblock");
+        const uint64_t root_oh = r.u64(fields + 32 + 8, -1, "root symbol table entry");
+
+        uint64_t btree = UNDEF, heap = UNDEF;
+        for (const MsgRef& m : header_messages(r, base, root_oh, -1))
+            if (m.type == 0x0011) {
+                btree = r.u64(m.off, -1, "symbol table message");
+                heap = r.u64(m.off + 8, -1, "symbol table message");
+            }
+        if (btree == UNDEF) throw H5Error{-1, "root group has no symbol table (new-style groups are not supported)"};
+        r.need(base + heap, 32, -1, "local heap");
+        if (std::memcmp(&r.b[base + heap], "HEAP", 4) != 0) throw H5Error{-1, "bad local heap signature"};
+        const uint64_t heap_data = r.u64(base + heap + 24, -1, "local heap");
+        std::vector<std::pair<std::string, uint64_t>> entries;
+        walk_group_btree(r, base, btree, heap_data, 0, entries);
+        uint64_t oh = UNDEF;
+        for (auto& e : entries)
+            if (e.first == name) oh = e.second;
+        if (oh == UNDEF) throw H5Error{-2, "no dataset named '" + name + "'"};
+
+        bool have_space = false, have_type = false, have_layout = false;
+        int cls = -1, size = 0;
+        bool be = false, sgn = false;
+        uint64_t daddr = UNDEF, dsize = 0, compact_off = UNDEF;
+        dims.clear();
+        for (const MsgRef& m : header_messages(r, base, oh, -2)) {
+            if (m.type == 0x0001) {
+                const int v = r.u8(m.off, -3, "dataspace"), nd = r.u8(m.off + 1, -3, "dataspace");
+                if (v == 2 && r.u8(m.off + 3, -3, "dataspace") == 2) throw H5Error{-3, "null dataspace"};
+                if (nd > 32) throw H5Error{-3, "dataspace rank above 32"};
+                const uint64_t q = m.off + (v == 1 ? 8 : 4);
+                for (int i = 0; i < nd; i++) dims.push_back(r.u64(q + 8ull * i, -3, "dataspace"));
+                have_space = true;
+            } else if (m.type == 0x0003) {
+                const uint8_t c0 = r.u8(m.off, -4, "datatype"), c1 = r.u8(m.off + 1, -4, "datatype");
+                cls = c0 & 0x0F;
+                size = (int)r.u32(m.off + 4, -4, "datatype");
+                be = (c1 & 1) != 0;
+                sgn = ((c1 >> 3) & 1) != 0;
+                if (cls == 1 && (size == 4 || size == 8) && !(c1 & 0x40)) {
+                    // IEEE single or double (not VAX order)
+                } else if (cls == 0 && size >= 1 && size <= 8) {
+                } else {
+                    throw H5Error{-4, "datatype class " + std::to_string(cls) + " size " + std::to_string(size) +
+                                          " is not an integer or IEEE float"};
+                }
+                have_type = true;
+            } else if (m.type == 0x0008) {
+                const int v = r.u8(m.off, -2, "layout");
+                if (v == 3) {
+                    const int lc = r.u8(m.off + 1, -2, "layout");
+                    if (lc == 1) {
+                        daddr = r.u64(m.off + 2, -2, "layout");
+                        dsize = r.u64(m.off + 10, -2, "layout");
+                    } else if (lc == 0) {
+                        dsize = r.u16(m.off + 2, -2, "layout");
+                        compact_off = m.off + 4;
+                    } else {
+                        throw H5Error{-2, "chunked or virtual layout is not supported"};
+                    }
+                } else if (v == 1 || v == 2) {
+                    const int nd = r.u8(m.off + 1, -2, "layout"), lc = r.u8(m.off + 2, -2, "layout");
+                    if (lc == 1) {
+                        daddr = r.u64(m.off + 8, -2, "layout");
+                        dsize = UNDEF;  // implied by dataspace and datatype
+                    } else if (lc == 0) {
+                        dsize = r.u32(m.off + 8 + 4ull * nd, -2, "layout");
+                        compact_off = m.off + 8 + 4ull * nd + 4;
+                    } else {
+                        throw H5Error{-2, "chunked layout is not supported"};
+                    }
+                } else {
+                    throw H5Error{-2, "layout message version " + std::to_string(v) + " is not supported"};
+                }
+                have_layout = true;
+            } else if (m.type == 0x000B) {
+                throw H5Error{-2, "filtered (compressed) datasets are not supported"};
+            }
+        }
+        if (!have_space) throw H5Error{-3, "dataset has no dataspace"};
+        if (!have_type) throw H5Error{-4, "dataset has no datatype"};
+        if (!have_layout) throw H5Error{-2, "dataset has no layout"};
+        uint64_t n = 1;
+        for (uint64_t d : dims) {
+            if (d && n > (1ull << 40) / d) throw H5Error{-3, "dataspace too large"};
+            n *= d;
+        }
+        const uint64_t bytes = n * (uint64_t)size;
+        if (dsize != UNDEF && dsize != bytes) throw H5Error{-3, "stored size does not match the dataspace"};
+        data.assign((size_t)n, 0.0);
+        uint64_t src = UNDEF;
+        if (compact_off != UNDEF) {
+            src = compact_off;
+        } else if (daddr != UNDEF) {
+            src = base + daddr;
+        }
+        if (src != UNDEF && n) {
+            r.need(src, bytes, -3, "dataset data");
+            for (uint64_t i = 0; i < n; i++) data[i] = to_double(&r.b[src + i * size], cls, size, be, sgn);
+        }
+        // An unallocated contiguous dataset reads as the default fill value 0.
+        if (type_class) *type_class = cls;
+        return 0;
+    } catch (const H5Error& e) {
+        if (why) *why = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        if (why) *why = "out of host memory";
+        return -3;
+    }
 }
 
 }  // namespace dg

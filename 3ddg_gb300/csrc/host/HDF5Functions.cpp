@@ -73,3 +73,30 @@ int hdf5outputScalar(const vector<vector<vector<double>>>& data3D, string output
     const long long dims[3] = {Dimx, Dimy, Dimz};
     return code_of(dg_hdf5_write(outputFilename.c_str(), Datasetname.c_str(), 3, dims, flat.data(), time));
 }
+
+int hdf5input(vector<vector<vector<double>>>& data3D, string inputFilename, string Datasetname, int Dimx, int Dimy,
+              int Dimz)
+{
+    static const char* const kind[5] = {"", "File", "DataSet", "DataSpace", "DataType"};
+    long long dims[32];
+    int nd = 0, cls = -1;
+    int rc = dg_hdf5_read(inputFilename.c_str(), Datasetname.c_str(), 32, dims, &nd, nullptr, 0, &cls);
+    long long n = 1;
+    for (int i = 0; i < nd && rc == 0; i++) n *= dims[i];
+    if (rc == 0 && n != (long long)Dimx * Dimy * Dimz) rc = -3;
+    std::vector<double> flat;
+    if (rc == 0) {
+        std::cout << cls << "\n";
+        flat.resize((size_t)n);
+        rc = dg_hdf5_read(inputFilename.c_str(), Datasetname.c_str(), 0, nullptr, nullptr, flat.data(), n, nullptr);
+    }
+    if (rc != 0) {
+        rc = code_of(rc);
+        std::cout << "HDF5 " << kind[-rc] << "IException error\n";
+        return rc;
+    }
+    for (int z = 0; z < Dimz; z++)
+        for (int y = 0; y < Dimy; y++)
+            for (int x = 0; x < Dimx; x++) data3D[x][y][z] = flat[((size_t)z * Dimy + y) * Dimx + x];
+    return 0;
+}

@@ -20,3 +20,11 @@ int hdf5outputVector(const vector<vector<vector<vector<double>>>>& data4D, strin
                      int Dimx, int Dimy, int Dimz, double time);
 int hdf5outputScalar(const vector<vector<vector<double>>>& data3D, string outputFilename, string Datasetname,
                      int Dimx, int Dimy, int Dimz, double time);
+// Reads dataset Datasetname, stored [Dimz][Dimy][Dimx] in row-major order, into
+// data3D[x][y][z] (data3D pre-sized [Dimx][Dimy][Dimz]) and prints the HDF5
+// datatype class; the reference's dormant restart reader
+// (cppsrc/HDF5Functions.cpp:398-463) with the same index mapping, messages and
+// return codes.  A dataset whose size differs from Dimx*Dimy*Dimz is a
+// dataspace error (-3) here, where the reference reads past its buffer.
+int hdf5input(vector<vector<vector<double>>>& data3D, string inputFilename, string Datasetname, int Dimx, int Dimy,
+              int Dimz);

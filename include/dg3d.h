@@ -176,6 +176,31 @@ int dg_write_snapshot(dg_handle* h, const char* folder, int ts, int grid);
 int dg_hdf5_write(const char* path, const char* name, int ndim, const long long* dims,
                   const double* data, double time);
 
+/* Read the numeric dataset ``name`` of an HDF5 file's root group, converted to
+ * float64 in row-major order; replaces the reference's dormant reader
+ * hdf5input (cppsrc/HDF5Functions.cpp:398-463; declared in
+ * HDF5Functions.h:26, no caller), without libhdf5.  Reads this library's files
+ * and the HDF5 library's default-format files: superblock 0/1, symbol-table
+ * root group, contiguous or compact layout, no filters, integer or IEEE float.
+ * *ndim receives the rank and dims[0..max_ndim-1] the leading dimensions;
+ * with data non-NULL the values are copied when they fit in ``capacity``
+ * doubles (else -3).  type_class (may be NULL) receives the HDF5 class, 0
+ * integer or 1 floating point.  Returns 0, or the reference's codes by failure
+ * class: -1 file, -2 dataset (no such name, chunked/filtered layout),
+ * -3 dataspace, -4 datatype; dg_last_error() says which.  Host only. */
+int dg_hdf5_read(const char* path, const char* name, int max_ndim, long long* dims, int* ndim,
+                 double* data, long long capacity, int* type_class);
+
+/* Restart from a snapshot (the use the reference's hdf5input was written for,
+ * cppsrc/HDF5Functions.cpp:398-463): read folder/raw/dRho_<b>_<ts>.h5 and
+ * vel_<b>_<ts>.h5 of every block, as dg_write_snapshot writes them, into the
+ * state (as dg_set_state does: boundary exterior values become zero) and set
+ * the simulation time to the files' "time".  An FP64 handle continues
+ * bit-identically to the run that wrote the snapshot.  Returns 0, the codes of
+ * dg_hdf5_read, or -3 when a file's shape does not match the grid.
+ * Synchronous. */
+int dg_read_snapshot(dg_handle* h, const char* folder, int ts);
+
 /* Pressure probes (no counterpart in the reference; for focal-axis and
  * harmonic analysis): after every subsequent RK step the pressure
  * p = c0^2 (drho + B/A drho^2 / (2 rho0)) at the node nearest to each of the n
