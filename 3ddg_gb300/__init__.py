@@ -83,6 +83,8 @@ def lib():
             "dg_dims": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
             "dg_get_state": (i, [vp, vp, vp]),
             "dg_set_state": (i, [vp, vp, vp]),
+            "dg_set_state_async": (i, [vp, vp, vp]),
+            "dg_get_state_async": (i, [vp, vp, vp]),
             "dg_eval_rhs": (i, [vp, vp, vp]),
             "dg_eval_rhs_noalloc": (i, [C.POINTER(DgParams), vp, vp, vp, vp, vp, vp, i, vp]),
             "dg_get_grid": (i, [vp, vp, vp]),
@@ -245,6 +247,22 @@ class Solver:
         rho = np.ascontiguousarray(rho, dtype=np.float64)
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         _check(lib().dg_set_state(self.h, _ptr(rho), _ptr(vel)), "dg_set_state")
+
+    def set_state_async(self, rho, vel):
+        """Queue an upload from pinned, C-contiguous float64 arrays; keep them
+        unchanged until ``synchronize``."""
+        for a in (rho, vel):
+            if not (a.flags.c_contiguous and a.dtype == np.float64):
+                raise DGError("set_state_async needs C-contiguous float64 arrays")
+        _check(lib().dg_set_state_async(self.h, _ptr(rho), _ptr(vel)), "dg_set_state_async")
+
+    def state_async(self, rho, vel):
+        """Queue a download into pinned, C-contiguous float64 arrays (either may
+        be None); they hold the state after ``synchronize``."""
+        for a in (rho, vel):
+            if a is not None and not (a.flags.c_contiguous and a.dtype == np.float64):
+                raise DGError("state_async needs C-contiguous float64 arrays")
+        _check(lib().dg_get_state_async(self.h, _ptr(rho), _ptr(vel)), "dg_get_state_async")
 
     def rhs(self):
         rho = np.empty(self.dims)

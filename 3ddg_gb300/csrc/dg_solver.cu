@@ -485,6 +485,95 @@ int Solver::unpack_in(const double* drho, const double* vel)
     return DG_OK;
 }
 
+int Solver::ensure_async()
+{
+    // Each resource is created once; a call after a failed one resumes here.
+    if (!copy_in) DG_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
+    if (!copy_out) DG_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++) {
+        if (!astage_in[i]) DG_CUDA(cudaMalloc(&astage_in[i], 4 * gsize() * sizeof(double)));
+        if (!astage_out[i]) DG_CUDA(cudaMalloc(&astage_out[i], 4 * gsize() * sizeof(double)));
+        for (cudaEvent_t* e : {&in_ready[i], &in_free[i], &out_ready[i], &out_free[i]})
+            if (!*e) DG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    return DG_OK;
+}
+
+// Upload on the copy-in stream into staging slot k, then unpack on the compute
+// stream.  The slot is reused only after the unpack that last read it.
+int Solver::set_state_async(const double* drho, const double* vel)
+{
+    if (!device_view(drho) || !device_view(vel))
+        return fail(DG_ERR_INVALID, "dg_set_state_async: host buffers must be page-locked (pinned)");
+    int rc = ensure_async();
+    if (rc) return rc;
+    const int k = in_slot;
+    in_slot ^= 1;
+    const size_t n = gsize();
+    double* st = astage_in[k];
+    DG_CUDA(cudaStreamWaitEvent(copy_in, in_free[k], 0));
+    DG_CUDA(cudaMemcpyAsync(st, drho, n * sizeof(double), cudaMemcpyHostToDevice, copy_in));
+    DG_CUDA(cudaMemcpyAsync(st + n, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, copy_in));
+    DG_CUDA(cudaEventRecord(in_ready[k], copy_in));
+    DG_CUDA(cudaStreamWaitEvent(stream, in_ready[k], 0));
+    const GridMap g = grid_map(mesh);
+    const int threads = 256, blocks = 152 * 16;
+    if (fp64()) {
+        unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
+                                                                         mesh.NP, g, st, st + n, n);
+    } else {
+        unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
+                                                                        g, st, st + n, n);
+        DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
+    }
+    launches++;
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaEventRecord(in_free[k], stream));
+    ic_live = false;
+    return DG_OK;
+}
+
+// Pack on the compute stream into staging slot k (after the download that last
+// read the slot), then download on the copy-out stream.
+int Solver::get_state_async(double* drho, double* vel)
+{
+    if ((drho && !device_view(drho)) || (vel && !device_view(vel)))
+        return fail(DG_ERR_INVALID, "dg_get_state_async: host buffers must be page-locked (pinned)");
+    int rc = ensure_async();
+    if (rc) return rc;
+    const int k = out_slot;
+    out_slot ^= 1;
+    const size_t n = gsize();
+    double* st = astage_out[k];
+    DG_CUDA(cudaStreamWaitEvent(stream, out_free[k], 0));
+    const GridMap g = grid_map(mesh);
+    const int threads = 256, blocks = 152 * 16;
+    if (fp64())
+        pack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((const double*)state_ptr(), mesh.fstride(),
+                                                                       mesh.NP, g, drho ? st : nullptr,
+                                                                       vel ? st + n : nullptr, n);
+    else
+        pack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((const float*)state_ptr(), mesh.fstride(),
+                                                                      mesh.NP, g, drho ? st : nullptr,
+                                                                      vel ? st + n : nullptr, n);
+    launches++;
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaEventRecord(out_ready[k], stream));
+    DG_CUDA(cudaStreamWaitEvent(copy_out, out_ready[k], 0));
+    if (drho) DG_CUDA(cudaMemcpyAsync(drho, st, n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
+    if (vel) DG_CUDA(cudaMemcpyAsync(vel, st + n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
+    DG_CUDA(cudaEventRecord(out_free[k], copy_out));
+    return DG_OK;
+}
+
+int Solver::sync_all()
+{
+    DG_CUDA(cudaStreamSynchronize(stream));
+    if (copy_in) DG_CUDA(cudaStreamSynchronize(copy_in));
+    if (copy_out) DG_CUDA(cudaStreamSynchronize(copy_out));
+    return DG_OK;
+}
+
 size_t Solver::device_bytes() const
 {
     const size_t fs = mesh.fstride();
@@ -604,6 +693,17 @@ void Solver::prof_reset()
 Solver::~Solver()
 {
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaStream_t c : {copy_in, copy_out})
+        if (c) {
+            cudaStreamSynchronize(c);
+            cudaStreamDestroy(c);
+        }
+    for (int i = 0; i < 2; i++) {
+        for (double* b : {astage_in[i], astage_out[i]})
+            if (b) cudaFree(b);
+        for (cudaEvent_t e : {in_ready[i], in_free[i], out_ready[i], out_free[i]})
+            if (e) cudaEventDestroy(e);
+    }
     prof_reset();
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
     for (void* b : buf)
@@ -663,9 +763,7 @@ int dg_step(dg_handle* h, double dt, int nsteps)
 int dg_synchronize(dg_handle* h)
 {
     if (!h) return fail(DG_ERR_INVALID, "dg_synchronize: null handle");
-    cudaError_t e = cudaStreamSynchronize(h->s.stream);
-    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
-    return DG_OK;
+    return h->s.sync_all();
 }
 
 int dg_dims(const dg_handle* h, int* X, int* Y, int* Z)
@@ -688,6 +786,18 @@ int dg_set_state(dg_handle* h, const double* drho, const double* vel)
 {
     if (!h || !drho || !vel) return fail(DG_ERR_INVALID, "dg_set_state: null argument");
     return h->s.unpack_in(drho, vel);
+}
+
+int dg_set_state_async(dg_handle* h, const double* drho, const double* vel)
+{
+    if (!h || !drho || !vel) return fail(DG_ERR_INVALID, "dg_set_state_async: null argument");
+    return h->s.set_state_async(drho, vel);
+}
+
+int dg_get_state_async(dg_handle* h, double* drho, double* vel)
+{
+    if (!h || (!drho && !vel)) return fail(DG_ERR_INVALID, "dg_get_state_async: null argument");
+    return h->s.get_state_async(drho, vel);
 }
 
 int dg_eval_rhs(dg_handle* h, double* drho, double* vel)

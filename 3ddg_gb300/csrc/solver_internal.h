@@ -79,6 +79,20 @@ struct Solver {
     int ensure_staging();
     int pack_out(const void* src, double* drho, double* vel);
     int unpack_in(const double* drho, const double* vel);
+
+    // Asynchronous host transfers (dg_set_state_async / dg_get_state_async):
+    // copy-engine streams and double-buffered device staging, so that one
+    // step's upload and the previous step's download run under compute.
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    double* astage_in[2] = {nullptr, nullptr};
+    double* astage_out[2] = {nullptr, nullptr};
+    cudaEvent_t in_ready[2] = {nullptr, nullptr}, in_free[2] = {nullptr, nullptr};
+    cudaEvent_t out_ready[2] = {nullptr, nullptr}, out_free[2] = {nullptr, nullptr};
+    int in_slot = 0, out_slot = 0;
+    int ensure_async();
+    int set_state_async(const double* drho, const double* vel);
+    int get_state_async(double* drho, double* vel);
+    int sync_all();
     ~Solver();
 };
 

@@ -43,13 +43,17 @@ def args_():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-extras", action="store_true", help="skip the FP32 form and error runs")
     ap.add_argument("--elements", type=int, default=0,
                     help="profiling cases only: the config2 physics on E^3 elements in one block")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--batch-steps", type=int, default=20, help="timed RK steps of the batched form")
+    ap.add_argument("--batch-instances", type=int, default=256,
+                    help="problems of the batched form (config 4 has 256; fewer only for profiling)")
+    ap.add_argument("--batch-tune-steps", type=int, default=2,
+                    help="RK steps per autotuner trial (0: no autotuning, default tiles)")
     ap.add_argument("--serve-requests", type=int, default=24, help="requests per arrival rate (serving form)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[5.0, 20.0, 50.0, 200.0])
     ap.add_argument("--serve-baseline-rates", type=float, nargs="*", default=[5.0, 200.0])
@@ -308,7 +312,9 @@ def run_ours(a, dist: Dist):
     value = dist.world * dofs / (ms_max / 1e3)
 
     # e2e through the public API with pinned host buffers: every step copies
-    # its input state host->device and its result device->host.
+    # its input state host->device and its result device->host.  The headline
+    # uses the asynchronous calls (copies on the copy engines, overlapping the
+    # neighbouring steps' compute); the synchronous calls are timed too.
     X, Y, Z = s.dims
     rho_t = torch.empty((X, Y, Z), dtype=torch.float64, pin_memory=True)
     vel_t = torch.empty((3, X, Y, Z), dtype=torch.float64, pin_memory=True)
@@ -322,13 +328,25 @@ def run_ours(a, dist: Dist):
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(ne2e):
-        s.set_state(rho, vel)
+        s.set_state_async(rho, vel)
         s.step(dt, 1)
-        s.state(rho_out, vel_out)
+        s.state_async(rho_out, vel_out)
+    s.synchronize()  # every copy has landed in host memory
     f1.record(stream)
     f1.synchronize()
     e2e_ms = dist.max(f0.elapsed_time(f1))
     e2e_value = dist.world * 4 * nodes * 3 * ne2e / (e2e_ms / 1e3)
+    dist.barrier()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(ne2e):
+        s.set_state(rho, vel)
+        s.step(dt, 1)
+        s.state(rho_out, vel_out)
+    g1.record(stream)
+    g1.synchronize()
+    sync_ms = dist.max(g0.elapsed_time(g1))
     step_bytes = 4 * nodes * 8
     s.close()
 
@@ -374,7 +392,12 @@ def run_ours(a, dist: Dist):
                    "l2": "inputs %s than L2 (state %.3g GB per buffer)" % ("larger" if buf_gb > 0.129 else "smaller",
                                                                           buf_gb), "dt_us": dt},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": step_bytes, "d2h_bytes_per_step": step_bytes,
-                "steps": ne2e, "ms_per_step": e2e_ms / ne2e},
+                "steps": ne2e, "ms_per_step": e2e_ms / ne2e,
+                "mode": "dg_set_state_async + dg_step + dg_get_state_async per step from/to pinned host buffers, "
+                        "timed from the first upload to the last download landing in host memory",
+                "sync_calls": {"value": dist.world * 4 * nodes * 3 * ne2e / (sync_ms / 1e3),
+                               "ms_per_step": sync_ms / ne2e,
+                               "mode": "dg_set_state + dg_step + dg_get_state (synchronous) per step"}},
         "gpu_launches": launches,
         "clocks": ck,
         "roofline": roof,
@@ -438,12 +461,12 @@ def precision_form(a, cfg, dg, W, torch):
 def batched_form(a, dg, W, torch):
     """Config 4: 256 uneven FP32 problems (N in 2..5) advanced together by one
     persistent kernel per RK stage under a CUDA graph; autotuned tiles."""
-    cfgs = W.config4(seed=0)
+    cfgs = W.config4(seed=0, n=a.batch_instances)
     steps = max(1, min(a.batch_steps, 400))
     with dg.Batch(cfgs) as b:
         nodes = b.total_nodes
         t0 = time.perf_counter()
-        tune = b.autotune(2)
+        tune = b.autotune(a.batch_tune_steps) if a.batch_tune_steps > 0 else "default tiles"
         tune_s = time.perf_counter() - t0
         stream = torch.cuda.ExternalStream(b.stream)
         b.step(a.warmup)
@@ -459,7 +482,8 @@ def batched_form(a, dg, W, torch):
     return {"value": 4 * nodes * 3 * steps / (ms / 1e3), "unit": UNIT, "problems": len(cfgs), "nodes": nodes,
             "orders": sorted({c["ORDER"] for c in cfgs}), "steps": steps, "ms_per_step": ms / steps,
             "autotune": tune, "autotune_s": tune_s, "graph_launches_per_step": launches / steps,
-            "workload": "config4: 256 instances, elements 4..24 per axis, N 2..5, FP32 Kahan, tone burst, sponge"}
+            "workload": "config4: %d instances, elements 4..24 per axis, N 2..5, FP32 Kahan, tone burst, sponge"
+                        % len(cfgs)}
 
 
 def serving_trace(rate: float, n: int, seed: int, W):

@@ -101,7 +101,8 @@ int dg_destroy(dg_handle* h);
  * on-device face gather.  Asynchronous on the handle's stream. */
 int dg_step(dg_handle* h, double dt, int nsteps);
 
-/* Wait for all work queued on the handle's stream. */
+/* Wait for all work queued on the handle: its compute stream and the copy
+ * streams of the asynchronous transfers. */
 int dg_synchronize(dg_handle* h);
 
 /* Node-duplicated global dimensions X = NB_x*E_x*(N+1), Y, Z: the array shape
@@ -116,6 +117,18 @@ int dg_get_state(dg_handle* h, double* drho, double* vel);
 /* Overwrite the current state from host buffers of the same layout.  Boundary
  * exterior values become zero (no initial-condition halo).  Synchronous. */
 int dg_set_state(dg_handle* h, const double* drho, const double* vel);
+
+/* Asynchronous forms of dg_set_state / dg_get_state for page-locked (pinned)
+ * host buffers (no counterpart in the reference, whose state never leaves the
+ * host).  The copies run on the copy engines through double-buffered device
+ * staging on two streams of their own, ordered against dg_step through
+ * events, so that the upload of the next input and the download of the last
+ * result overlap the steps computing between them.  dg_get_state_async
+ * captures the state at its place in the call sequence.  Host buffers must
+ * stay untouched (inputs) or unread (outputs) until dg_synchronize returns.
+ * Pageable buffers are rejected with DG_ERR_INVALID. */
+int dg_set_state_async(dg_handle* h, const double* drho, const double* vel);
+int dg_get_state_async(dg_handle* h, double* drho, double* vel);
 
 /* One evaluation R = L(u) of the semi-discrete right-hand side at the current
  * state (LDG diffusion, advection, sponge; no RK combination) into host

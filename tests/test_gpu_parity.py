@@ -197,3 +197,41 @@ def test_fp32_form_within_tolerance(solver_for, oracle_for):
     p_g, p_o = pressure(cfg, r_g), pressure(cfg, r_o)
     l2 = np.linalg.norm(p_g - p_o) / np.linalg.norm(p_o)
     assert l2 <= 1e-5, l2
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_async_transfers_match_sync(precision, solver_for):
+    """dg_set_state_async / dg_get_state_async pipelined over several steps give
+    the same bytes as the synchronous calls; pageable buffers are refused."""
+    import torch
+    m = __import__("conftest").dg()
+    cfg = small(order=3, ne=(3, 4, 2))
+    cfg["PRECISION"] = precision
+    a, b = solver_for(cfg), solver_for(cfg)
+    shape = a.dims
+    rng = np.random.default_rng(11)
+
+    def pinned(shp):
+        return torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
+
+    ins, outs = [], []
+    for k in range(3):
+        r, v = pinned(shape), pinned((3,) + shape)
+        r[...] = rng.standard_normal(shape) * 1e-3
+        v[...] = rng.standard_normal((3,) + shape) * 1e-6
+        ins.append((r, v))
+        outs.append((pinned(shape), pinned((3,) + shape)))
+    for k in range(3):
+        a.set_state_async(*ins[k])
+        a.step(cfg["DT"], 2)
+        a.state_async(*outs[k])
+    a.synchronize()
+    for k in range(3):
+        b.set_state(*ins[k])
+        b.step(cfg["DT"], 2)
+        r, v = b.state()
+        assert np.array_equal(r, outs[k][0]) and np.array_equal(v, outs[k][1])
+    with pytest.raises(m.DGError, match="page-locked"):
+        a.set_state_async(np.zeros(shape), np.zeros((3,) + shape))
+    with pytest.raises(m.DGError, match="page-locked"):
+        a.state_async(np.zeros(shape), None)
