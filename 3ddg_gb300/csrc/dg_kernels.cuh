@@ -194,8 +194,17 @@ struct OpRows {
     }
 };
 
+// Resident CTAs per SM asked of the compiler for the gradient kernel (0: no
+// request): the FP32 kernel waits on memory latency and fits in 40 registers
+// without spilling up to K = 5.
+template <typename T, int K>
+__host__ __device__ constexpr int grad_min_blocks()
+{
+    return (sizeof(T) == 4 && K <= 5) ? 65536 / (40 * npt_of(K) * epb_of(K)) : 0;
+}
+
 template <typename T, int K, bool INCR>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (grad_min_blocks<T, K>()))
 ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp)
 {
     constexpr int K2 = K * K, K3 = K * K * K;
@@ -207,25 +216,60 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     const bool act = n < K3 && e < m.n_elem;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     OpRows<T, K> R;
-    R.load(C, c, act);
     T rho = T(0);
-    if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
-    S.r[n] = rho;
-    if (act) {
+    if constexpr (INCR) {
+        // FP32 (latency-bound): face-table codes first, so that the neighbour
+        // loads that depend on them are issued together with the own load.
+        int code[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            if (act && (c[a] == 0 || c[a] == K - 1))
+                code[a] = __ldg(m.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
+        T ro[3] = {T(0), T(0), T(0)};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            if (c[a] != 0 && c[a] != K - 1) continue;
+            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
             const int side = c[a] == 0 ? 0 : 1;
-            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-            const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * a + side);
-            T ro, uo;
-            if (code >= 0) {
+            if (code[a] >= 0) {
                 const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                ro = load_in<INCR>(io, 0, (size_t)code * io.np + nn);
+                ro[a] = load_in<INCR>(io, 0, (size_t)code[a] * io.np + nn);
             } else {
-                exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
+                T uo;
+                exterior<T, K>(m, C, -1 - code[a], side, c[(a + 1) % 3] * K + c[(a + 2) % 3], ro[a], uo);
             }
-            S.fl[a][side][fi] = C.cQ[a][side] * (ro + rho);
+        }
+        R.load(C, c, act);
+        S.r[n] = rho;
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (c[a] != 0 && c[a] != K - 1) continue;
+                const int side = c[a] == 0 ? 0 : 1;
+                S.fl[a][side][c[(a + 1) % 3] * K + c[(a + 2) % 3]] = C.cQ[a][side] * (ro[a] + rho);
+            }
+        }
+    } else {
+        // FP64 (bound by the FP64 pipe): loads in program order.
+        R.load(C, c, act);
+        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
+        S.r[n] = rho;
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (c[a] != 0 && c[a] != K - 1) continue;
+                const int side = c[a] == 0 ? 0 : 1;
+                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * a + side);
+                T ro, uo;
+                if (code >= 0) {
+                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+                    ro = load_in<INCR>(io, 0, (size_t)code * io.np + nn);
+                } else {
+                    exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
+                }
+                S.fl[a][side][fi] = C.cQ[a][side] * (ro + rho);
+            }
         }
     }
     __syncthreads();
@@ -246,22 +290,11 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// One RK stage: R = L(stage input), then the stage combination.
+// One RK stage of the plain (FP64) form: R = L(stage input), then the stage
+// combination dst = R' + s (cb - ca sigma) + cc old.
 // ---------------------------------------------------------------------------
-// Resident CTAs per SM asked of the compiler (0: no request).  The FP32 stage
-// kernel waits on global loads (long-scoreboard stalls), so where the
-// compiler can fit it in fewer registers without spilling it trades them for
-// resident warps: 40 registers at K = 2, 48 at K = 5 (the common N = 4).  The
-// FP64 kernel is bound by the FP64 pipe and keeps its registers.
-template <typename T, int K>
-__host__ __device__ constexpr int stage_min_blocks()
-{
-    return sizeof(T) != 4 ? 0 : (K == 2 ? 65536 / (40 * npt_of(K) * epb_of(K))
-                                        : (K == 5 ? 65536 / (48 * npt_of(K) * epb_of(K)) : 0));
-}
-
-template <typename T, int K, bool DIFF, bool INCR>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (stage_min_blocks<T, K>()))
+template <typename T, int K, bool DIFF>
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
     constexpr int K2 = K * K, K3 = K * K * K;
@@ -278,9 +311,9 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 
     T rho = T(0), u[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     if (act) {
-        rho = load_in<INCR>(io, 0, off);
+        rho = load_in<false>(io, 0, off);
 #pragma unroll
-        for (int a = 0; a < 3; a++) u[a] = load_in<INCR>(io, 1 + a, off);
+        for (int a = 0; a < 3; a++) u[a] = load_in<false>(io, 1 + a, off);
         if (DIFF)
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
@@ -311,8 +344,8 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
             if (code >= 0) {
                 const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
                 const size_t o2 = (size_t)code * io.np + nn;
-                ro = load_in<INCR>(io, 0, o2);
-                uo = load_in<INCR>(io, 1 + a, o2);
+                ro = load_in<false>(io, 0, o2);
+                uo = load_in<false>(io, 1 + a, o2);
                 if (DIFF) qo = __ldg(io.q + (size_t)a * io.fs + o2);
             } else {
                 exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
@@ -356,33 +389,148 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);
 
     const T r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
-    if (!INCR) {
-        const T s4[4] = {rho, u[0], u[1], u[2]};
-        const T cbe = io.cb - ks;
+    const T s4[4] = {rho, u[0], u[1], u[2]};
+    const T cbe = io.cb - ks;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        const size_t o = (size_t)f * io.fs + off;
+        T v = r[f] + s4[f] * cbe;
+        if (io.old) v += io.old[o] * io.cc;
+        io.dst[o] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One RK stage of the increment (FP32) form, arranged so that every global
+// load a thread makes is issued before the first value is used: the
+// neighbour codes and sigma, the thread's own u, d, gradient and Kahan
+// compensation, and then the neighbour values across its faces.  The kernel
+// waits on memory latency, so the loads wait together instead of in four
+// dependent waves (own state, face table, neighbour values, reloads of u and
+// d for the update).
+// ---------------------------------------------------------------------------
+template <typename T, int K, bool DIFF>
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
+incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
+{
+    constexpr int K2 = K * K, K3 = K * K * K;
+    __shared__ StageSmem<T, K> sm_all[epb_of(K)];
+    StageSmem<T, K>& S = sm_all[threadIdx.y];
+    const OpConst<T, K>& C = *Cp;
+    const int n = threadIdx.x;
+    const int e = blockIdx.x * epb_of(K) + threadIdx.y;
+    const bool act = n < K3 && e < m.n_elem;
+    const int c[3] = {n / K2, (n / K) % K, n % K};
+    const size_t off = (size_t)e * io.np + n;
+
+    bool on[3];
+    int code[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        on[a] = act && (c[a] == 0 || c[a] == K - 1);
+        if (on[a]) code[a] = __ldg(m.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+    }
+    const T sig = (act && do_sponge) ? __ldg(m.sigma + e) : T(0);
+    T ub[4] = {T(0), T(0), T(0), T(0)}, dv[4] = {T(0), T(0), T(0), T(0)};
+    T cmp[4] = {T(0), T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
+    if (act) {
 #pragma unroll
         for (int f = 0; f < 4; f++) {
-            const size_t o = (size_t)f * io.fs + off;
-            T v = r[f] + s4[f] * cbe;
-            if (io.old) v += io.old[o] * io.cc;
-            io.dst[o] = v;
+            ub[f] = __ldg(io.src + (size_t)f * io.fs + off);
+            if (io.inc) dv[f] = __ldg(io.inc + (size_t)f * io.fs + off);
+            if (io.final_stage) cmp[f] = io.comp[(size_t)f * io.fs + off];
         }
-    } else {
-        const T cbe = io.cb - ks, ce = io.eps - ks;
+        if (DIFF)
 #pragma unroll
-        for (int f = 0; f < 4; f++) {
-            const size_t o = (size_t)f * io.fs + off;
-            const T ub = __ldg(io.src + o);
-            T d = r[f] + ub * ce;
-            if (io.inc) d += __ldg(io.inc + o) * cbe;
-            if (io.final_stage) {
-                // Kahan-compensated u <- u + d
-                const T y = d - io.comp[o];
-                const T t = ub + y;
-                io.comp[o] = (t - ub) - y;
-                io.dst[o] = t;
-            } else {
-                io.dst[o] = d;
-            }
+            for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
+    }
+    OpRows<T, K> R;
+    R.load(C, c, act);
+
+    T ro[3], uo[3], qo[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        ro[a] = uo[a] = qo[a] = T(0);
+        if (!on[a]) continue;
+        const int side = c[a] == 0 ? 0 : 1;
+        if (code[a] >= 0) {
+            const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+            const size_t o2 = (size_t)code[a] * io.np + nn;
+            ro[a] = load_in<true>(io, 0, o2);
+            uo[a] = load_in<true>(io, 1 + a, o2);
+            if (DIFF) qo[a] = __ldg(io.q + (size_t)a * io.fs + o2);
+        } else {
+            exterior<T, K>(m, C, -1 - code[a], side, c[(a + 1) % 3] * K + c[(a + 2) % 3], ro[a], uo[a]);
+        }
+    }
+
+    const T rho = ub[0] + dv[0];
+    const T u[3] = {ub[1] + dv[1], ub[2] + dv[2], ub[3] + dv[3]};
+    T fmom = T(0), fmass[3] = {T(0), T(0), T(0)};
+    if (do_adv) {
+        fmom = momentum_flux(rho, C.k1, C.k2);
+#pragma unroll
+        for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, C.r0, C.linear_mass);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        S.f[a][n].x = fmom;
+        S.f[a][n].y = DIFF ? fmass[a] + q[a] : fmass[a];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (!on[a]) continue;
+        const int side = c[a] == 0 ? 0 : 1;
+        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+        T gm = T(0), gr = T(0);
+        if (do_adv) {
+            const T fmo = momentum_flux(ro[a], C.k1, C.k2);
+            const T fao = mass_flux(uo[a], ro[a], C.r0, C.linear_mass);
+            const T* cm = C.cM[a][side];
+            const T* cr = C.cA[a][side];
+            gm = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
+            gr = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3];
+        }
+        if (DIFF) gr += C.cQ[a][side] * (qo[a] + q[a]);
+        S.g[a][side][fi].x = gm;
+        S.g[a][side][fi].y = gr;
+    }
+    __syncthreads();
+    if (!act) return;
+
+    T r[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int st = axis_stride<K>(a), base = n - c[a] * st;
+        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+        const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
+        T sm = R.l0[a] * g0.x, sr = R.l0[a] * g0.y;
+        sm += R.ln[a] * gN.x;
+        sr += R.ln[a] * gN.y;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            const typename Pair<T>::type v = S.f[a][base + j * st];
+            sm += R.d[a][j] * v.x;
+            sr += R.d[a][j] * v.y;
+        }
+        r[0] += sr;
+        r[1 + a] = do_adv ? sm : T(0);
+    }
+    const T ks = io.ca * sig;
+    const T cbe = io.cb - ks, ce = io.eps - ks;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        const size_t o = (size_t)f * io.fs + off;
+        T d = r[f] + ub[f] * ce;
+        if (io.inc) d += dv[f] * cbe;
+        if (io.final_stage) {
+            // Kahan-compensated u <- u + d
+            const T y = d - cmp[f];
+            const T t = ub[f] + y;
+            io.comp[o] = (t - ub[f]) - y;
+            io.dst[o] = t;
+        } else {
+            io.dst[o] = d;
         }
     }
 }

@@ -145,10 +145,17 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slo
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(0, &ev);
-    if (s.p.eval_diff)
-        stage_kernel<T, K, true, INCR><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
-    else
-        stage_kernel<T, K, false, INCR><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+    if constexpr (INCR) {
+        if (s.p.eval_diff)
+            incr_stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+        else
+            incr_stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+    } else {
+        if (s.p.eval_diff)
+            stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+        else
+            stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+    }
     s.prof_end(0, ev, stage_bytes<T, INCR>(s, io), stage_flops(s, io.old != nullptr || io.inc != nullptr));
     s.launches++;
 }
