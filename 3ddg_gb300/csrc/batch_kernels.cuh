@@ -58,24 +58,36 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
         const int e = c0 + slot;
         const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
         GradSmem<float, K>& S = SM[slot < EPB ? slot : 0];
+        // Face-table codes first, so that the neighbour loads that depend on
+        // them are issued together with the own load (the kernel waits on
+        // memory latency).
+        int code[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            if (act && (c[a] == 0 || c[a] == K - 1))
+                code[a] = __ldg(P.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
         float rho = 0.f;
         if (act) rho = batch_in<K>(P, ub, inc, 0, (size_t)e * P.np + n);
+        float ro[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
+            const int side = c[a] == 0 ? 0 : 1;
+            if (code[a] >= 0) {
+                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+                ro[a] = batch_in<K>(P, ub, inc, 0, (size_t)code[a] * P.np + nn);
+            } else {
+                float uo;
+                batch_exterior(P, -1 - code[a], stage, ro[a], uo);
+            }
+        }
         if (slot < EPB) S.r[n] = rho;
         if (act) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 if (c[a] != 0 && c[a] != K - 1) continue;
                 const int side = c[a] == 0 ? 0 : 1;
-                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                const int code = __ldg(P.nbr + (size_t)e * 6 + 2 * a + side);
-                float ro, uo;
-                if (code >= 0) {
-                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                    ro = batch_in<K>(P, ub, inc, 0, (size_t)code * P.np + nn);
-                } else {
-                    batch_exterior(P, -1 - code, stage, ro, uo);
-                }
-                S.fl[a][side][fi] = (side ? -0.5f : 0.5f) * (ro + rho);
+                S.fl[a][side][c[(a + 1) % 3] * K + c[(a + 2) % 3]] = (side ? -0.5f : 0.5f) * (ro[a] + rho);
             }
         }
         __syncthreads();
@@ -112,15 +124,44 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
         const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
         StageSmem<float, K>& S = SM[slot < EPB ? slot : 0];
         const size_t off = (size_t)e * P.np + n;
-        float rho = 0.f, u[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
-        if (act) {
-            rho = batch_in<K>(P, ub, inc, 0, off);
+        // Every global load before the first use (the kernel waits on memory
+        // latency): face-table codes and sigma, the own u, d, gradient and
+        // compensation, then the neighbour values across the node's faces.
+        int code[3] = {0, 0, 0};
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                u[a] = batch_in<K>(P, ub, inc, 1 + a, off);
-                q[a] = __ldg(P.q + (size_t)a * P.fs + off);
+        for (int a = 0; a < 3; a++)
+            if (act && (c[a] == 0 || c[a] == K - 1))
+                code[a] = __ldg(P.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+        const float sig = act ? __ldg(P.sigma + e) : 0.f;
+        float ubv[4] = {0.f, 0.f, 0.f, 0.f}, dv[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+        float q[3] = {0.f, 0.f, 0.f};
+        if (act) {
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                ubv[f] = __ldg(ub + (size_t)f * P.fs + off);
+                if (inc) dv[f] = __ldg(inc + (size_t)f * P.fs + off);
+                if (final_stage) cmp[f] = P.comp[(size_t)f * P.fs + off];
+            }
+#pragma unroll
+            for (int a = 0; a < 3; a++) q[a] = __ldg(P.q + (size_t)a * P.fs + off);
+        }
+        float ro[3] = {0.f, 0.f, 0.f}, uo[3] = {0.f, 0.f, 0.f}, qo[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
+            const int side = c[a] == 0 ? 0 : 1;
+            if (code[a] >= 0) {
+                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
+                const size_t o2 = (size_t)code[a] * P.np + nn;
+                ro[a] = batch_in<K>(P, ub, inc, 0, o2);
+                uo[a] = batch_in<K>(P, ub, inc, 1 + a, o2);
+                qo[a] = __ldg(P.q + (size_t)a * P.fs + o2);
+            } else {
+                batch_exterior(P, -1 - code[a], stage, ro[a], uo[a]);
             }
         }
+        const float rho = ubv[0] + dv[0];
+        const float u[3] = {ubv[1] + dv[1], ubv[2] + dv[2], ubv[3] + dv[3]};
         const float fmom = momentum_flux(rho, P.k1, P.k2);
         float fmass[3];
 #pragma unroll
@@ -135,24 +176,13 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
                 if (c[a] != 0 && c[a] != K - 1) continue;
                 const int side = c[a] == 0 ? 0 : 1;
                 const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                const int code = __ldg(P.nbr + (size_t)e * 6 + 2 * a + side);
-                float ro, uo, qo = 0.f;
-                if (code >= 0) {
-                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                    const size_t o2 = (size_t)code * P.np + nn;
-                    ro = batch_in<K>(P, ub, inc, 0, o2);
-                    uo = batch_in<K>(P, ub, inc, 1 + a, o2);
-                    qo = __ldg(P.q + (size_t)a * P.fs + o2);
-                } else {
-                    batch_exterior(P, -1 - code, stage, ro, uo);
-                }
-                const float fmo = momentum_flux(ro, P.k1, P.k2);
-                const float fao = mass_flux(uo, ro, P.r0, P.linear_mass);
+                const float fmo = momentum_flux(ro[a], P.k1, P.k2);
+                const float fao = mass_flux(uo[a], ro[a], P.r0, P.linear_mass);
                 const float* cm = P.cM[side];
                 const float* cr = P.cA[side];
                 S.g[a][side][fi] = make_float2(fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3],
                                                fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3] +
-                                                   (side ? -0.5f : 0.5f) * (qo + q[a]));
+                                                   (side ? -0.5f : 0.5f) * (qo[a] + q[a]));
             }
         }
         __syncthreads();
@@ -176,19 +206,18 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
                 r_rho += P.invw[a] * sr;
                 r_u[a] = P.invw[a] * sm;
             }
-            const float ks = ca * __ldg(P.sigma + e);
+            const float ks = ca * sig;
             const float cbe = cb - ks, ce = eps - ks;
             const float r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
 #pragma unroll
             for (int f = 0; f < 4; f++) {
                 const size_t o = (size_t)f * P.fs + off;
-                const float ubv = __ldg(ub + o);
-                float d = ca * r[f] + ubv * ce;
-                if (inc) d += __ldg(inc + o) * cbe;
+                float d = ca * r[f] + ubv[f] * ce;
+                if (inc) d += dv[f] * cbe;
                 if (final_stage) {
-                    const float y = d - P.comp[o];
-                    const float t = ubv + y;
-                    P.comp[o] = (t - ubv) - y;
+                    const float y = d - cmp[f];
+                    const float t = ubv[f] + y;
+                    P.comp[o] = (t - ubv[f]) - y;
                     dout[o] = t;
                 } else {
                     dout[o] = d;
