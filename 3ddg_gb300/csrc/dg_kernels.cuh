@@ -40,16 +40,38 @@ namespace dg {
 __host__ __device__ constexpr int npt_of(int K) { return (K * K * K + 31) / 32 * 32; }
 __host__ __device__ constexpr int epb_of(int K) { return K <= 3 ? 4 : (K == 4 ? 2 : 1); }
 
-// Per-launch operator constants, passed by value (kernel parameter space).
+// A 16-byte vector of T (the widest per-thread global load).
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+};
+
+// Length of one operator row: K entries of D, the two lift entries, padded to
+// whole 16-byte vectors.
+template <typename T, int K>
+__host__ __device__ constexpr int oprow_len()
+{
+    return (K + 2 + (int)(16 / sizeof(T)) - 1) / (int)(16 / sizeof(T)) * (int)(16 / sizeof(T));
+}
+
+// Per-launch operator constants, in device memory.
 //   stage kernel:    D[a] = ca D / w_a;   cM, cA: face coefficients of the
 //                    momentum / mass equations times ca * (lift scale);
 //                    cQ[a] = (+0.5, -0.5) ca / w_a (central flux of G).
 //   gradient kernel: D[a] = D_c D / w_a;  cQ[a] = (+0.5, -0.5) D_c / w_a.
+// rows[a][i] = (D[a][i][0..K-1], L0[i], LN[i], 0...) with the lift columns
+// L0 = M^-1 e_0, LN = M^-1 e_N, so that a thread loads its row of each axis
+// with one or two 16-byte loads.
 // Face coefficients act on (f_mom other, f_mom self, f_mass other, f_mass self).
 template <typename T, int K>
 struct OpConst {
-    T D[3][K][K];
-    T L0[K], LN[K];        // lift columns M^-1 e_0, M^-1 e_N
+    alignas(16) T rows[3][K][oprow_len<T, K>()];
     T cM[3][2][4];
     T cA[3][2][4];
     T cQ[3][2];
@@ -183,13 +205,19 @@ struct OpRows {
     T d[3][K], l0[3], ln[3];
     __device__ __forceinline__ void load(const OpConst<T, K>& C, const int c[3], bool act)
     {
+        using V = typename Vec16<T>::type;
+        constexpr int RL = oprow_len<T, K>(), NV = RL * (int)sizeof(T) / 16;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
             const int ia = act ? c[a] : 0;
-            l0[a] = C.L0[ia];
-            ln[a] = C.LN[ia];
+            T row[RL];
+            const V* src = reinterpret_cast<const V*>(C.rows[a][ia]);
 #pragma unroll
-            for (int j = 0; j < K; j++) d[a][j] = C.D[a][ia][j];
+            for (int v = 0; v < NV; v++) reinterpret_cast<V*>(row)[v] = __ldg(src + v);
+#pragma unroll
+            for (int j = 0; j < K; j++) d[a][j] = row[j];
+            l0[a] = row[K];
+            ln[a] = row[K + 1];
         }
     }
 };
@@ -544,10 +572,11 @@ inline OpConst<T, K> make_stage_const(double rk_ca, const double* deriv, const d
                                       double diff_const)
 {
     OpConst<T, K> C{};
-    for (int i = 0; i < K; i++) {
-        C.L0[i] = (T)lift0[i];
-        C.LN[i] = (T)liftN[i];
-    }
+    for (int a = 0; a < 3; a++)
+        for (int i = 0; i < K; i++) {
+            C.rows[a][i][K] = (T)lift0[i];
+            C.rows[a][i][K + 1] = (T)liftN[i];
+        }
     // Face-flux coefficients as the reference forms them (cppsrc/Element.cpp:542-556
     // left, :581-595 right); z = rho0 c0 and r = rho0 on both sides.
     const double r0 = rho0, z1 = r0 * c0, z2 = r0 * c0, r1 = r0, r2 = r0;
@@ -559,7 +588,7 @@ inline OpConst<T, K> make_stage_const(double rk_ca, const double* deriv, const d
     const double cR1[4] = {z1 / r1 / (z1 + z2), z2 / r2 / (z1 + z2), r1 / (z1 + z2), -1.0 * r2 / (z1 + z2)};
     for (int a = 0; a < 3; a++) {
         for (int i = 0; i < K; i++)
-            for (int j = 0; j < K; j++) C.D[a][i][j] = (T)(rk_ca * deriv[i * K + j] / w[a]);
+            for (int j = 0; j < K; j++) C.rows[a][i][j] = (T)(rk_ca * deriv[i * K + j] / w[a]);
         // momentum: lift scale -1/(rho0 w); left flux F_0 = -(fmo cL0[0] + fms cL0[1]
         // + fao cL0[2] + fas cL0[3]), right F_N = fms cR0[0] + fmo cR0[1] + fas cR0[2] + fao cR0[3]
         const double km = rk_ca * (-1.0 / (r0 * w[a]));
@@ -595,13 +624,12 @@ inline OpConst<T, K> make_grad_const(const double* deriv, const double* lift0, c
                                      const double w[3], double rho0, double c0, double diff_const)
 {
     OpConst<T, K> C{};
-    for (int i = 0; i < K; i++) {
-        C.L0[i] = (T)lift0[i];
-        C.LN[i] = (T)liftN[i];
-    }
     for (int a = 0; a < 3; a++) {
-        for (int i = 0; i < K; i++)
-            for (int j = 0; j < K; j++) C.D[a][i][j] = (T)(diff_const * deriv[i * K + j] / w[a]);
+        for (int i = 0; i < K; i++) {
+            for (int j = 0; j < K; j++) C.rows[a][i][j] = (T)(diff_const * deriv[i * K + j] / w[a]);
+            C.rows[a][i][K] = (T)lift0[i];
+            C.rows[a][i][K + 1] = (T)liftN[i];
+        }
         C.cQ[a][0] = (T)(0.5 * diff_const / w[a]);
         C.cQ[a][1] = (T)(-0.5 * diff_const / w[a]);
     }
