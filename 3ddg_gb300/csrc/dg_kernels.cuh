@@ -656,32 +656,46 @@ __device__ __forceinline__ size_t grid_index(const GridMap& g, int e, int n)
     return (ii * ((size_t)g.E[1] * K) + jj) * ((size_t)g.E[2] * K) + kk;
 }
 
-// Element-major offset (e * NP + n) of the node at node-duplicated position
-// (ii, jj, kk): the inverse of grid_index.
-__device__ __forceinline__ size_t elem_offset(const GridMap& g, int np, size_t ii, size_t jj, size_t kk)
-{
-    const int K = g.K;
-    const int gx = (int)(ii / K), gy = (int)(jj / K), gz = (int)(kk / K);
-    const int a = (int)(ii % K), b = (int)(jj % K), c = (int)(kk % K);
-    const int bx = gx / g.ne[0], by = gy / g.ne[1], bz = gz / g.ne[2];
-    const int lx = gx % g.ne[0], ly = gy % g.ne[1], lz = gz % g.ne[2];
-    const size_t e = (size_t)((bx * g.nb[1] + by) * g.nb[2] + bz) * g.elem_per_block + (lx * g.ne[1] + ly) * g.ne[2] + lz;
-    return e * np + (a * K + b) * K + c;
-}
-
 // State <-> host-order arrays rho [X][Y][Z], vel [3][X][Y][Z], walked in host
 // order so that rho/vel may be pinned host memory read or written directly by
-// the kernel (streaming, coalesced on the host side), or device staging.
+// the kernel (streaming, coalesced on the host side), or device staging.  A
+// CTA takes one (x, y) row at a time and its threads walk z, so the element
+// arithmetic is 32-bit and mostly per row.
+struct RowMap {
+    int elem_xy;  // element-index part of the row's element coordinates
+    int node_xy;  // (a K + b) K: node-index part of the row
+};
+
+__device__ __forceinline__ RowMap row_map(const GridMap& g, int ii, int jj)
+{
+    const int K = g.K;
+    const int gx = ii / K, gy = jj / K;
+    const int bx = gx / g.ne[0], by = gy / g.ne[1], lx = gx % g.ne[0], ly = gy % g.ne[1];
+    return {(bx * g.nb[1] + by) * g.nb[2] * g.elem_per_block + (lx * g.ne[1] + ly) * g.ne[2],
+            ((ii % K) * K + jj % K) * K};
+}
+
+__device__ __forceinline__ size_t row_offset(const GridMap& g, int np, const RowMap& r, int kk)
+{
+    const int gz = kk / g.K;
+    const int e = r.elem_xy + (gz / g.ne[2]) * g.elem_per_block + gz % g.ne[2];
+    return (size_t)e * np + r.node_xy + kk % g.K;
+}
+
 template <typename T>
 __global__ void pack_host_order_kernel(const T* __restrict__ state, size_t fs, int np, GridMap g,
                                        double* __restrict__ rho, double* __restrict__ vel, size_t gsize)
 {
-    const size_t Y = (size_t)g.E[1] * g.K, Z = (size_t)g.E[2] * g.K;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < gsize; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t o = elem_offset(g, np, i / (Y * Z), (i / Z) % Y, i % Z);
-        if (rho) rho[i] = (double)state[o];
-        if (vel)
-            for (int a = 0; a < 3; a++) vel[a * gsize + i] = (double)state[(size_t)(1 + a) * fs + o];
+    const int Y = g.E[1] * g.K, Z = g.E[2] * g.K, rows = g.E[0] * g.K * Y;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const RowMap r = row_map(g, row / Y, row % Y);
+        for (int kk = threadIdx.x; kk < Z; kk += blockDim.x) {
+            const size_t o = row_offset(g, np, r, kk), i = (size_t)row * Z + kk;
+            if (rho) rho[i] = (double)state[o];
+            if (vel)
+#pragma unroll
+                for (int a = 0; a < 3; a++) vel[a * gsize + i] = (double)state[(size_t)(1 + a) * fs + o];
+        }
     }
 }
 
@@ -689,11 +703,15 @@ template <typename T>
 __global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g,
                                          const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize)
 {
-    const size_t Y = (size_t)g.E[1] * g.K, Z = (size_t)g.E[2] * g.K;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < gsize; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t o = elem_offset(g, np, i / (Y * Z), (i / Z) % Y, i % Z);
-        state[o] = (T)rho[i];
-        for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + o] = (T)vel[a * gsize + i];
+    const int Y = g.E[1] * g.K, Z = g.E[2] * g.K, rows = g.E[0] * g.K * Y;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const RowMap r = row_map(g, row / Y, row % Y);
+        for (int kk = threadIdx.x; kk < Z; kk += blockDim.x) {
+            const size_t o = row_offset(g, np, r, kk), i = (size_t)row * Z + kk;
+            state[o] = (T)rho[i];
+#pragma unroll
+            for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + o] = (T)vel[a * gsize + i];
+        }
     }
 }
 

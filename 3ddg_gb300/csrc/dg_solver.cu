@@ -435,7 +435,7 @@ const void* device_view(const void* host)
 int Solver::pack_out(const void* src, double* drho, double* vel)
 {
     const GridMap g = grid_map(mesh);
-    const int threads = 256, blocks = 152 * 16;
+    const int threads = 128, blocks = 152 * 16;
     double* rho_d = (double*)device_view(drho);
     double* vel_d = (double*)device_view(vel);
     const bool direct = (!drho || rho_d) && (!vel || vel_d);
@@ -466,7 +466,7 @@ int Solver::pack_out(const void* src, double* drho, double* vel)
 int Solver::unpack_in(const double* drho, const double* vel)
 {
     const GridMap g = grid_map(mesh);
-    const int threads = 256, blocks = 152 * 16;
+    const int threads = 128, blocks = 152 * 16;
     const double* rho_d = (const double*)device_view(drho);
     const double* vel_d = (const double*)device_view(vel);
     if (!rho_d || !vel_d) {
@@ -524,7 +524,7 @@ int Solver::set_state_async(const double* drho, const double* vel)
     DG_CUDA(cudaEventRecord(in_ready[k], copy_in));
     DG_CUDA(cudaStreamWaitEvent(stream, in_ready[k], 0));
     const GridMap g = grid_map(mesh);
-    const int threads = 256, blocks = 152 * 16;
+    const int threads = 128, blocks = 152 * 16;
     if (fp64()) {
         unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
                                                                          mesh.NP, g, st, st + n, n);
@@ -554,7 +554,7 @@ int Solver::get_state_async(double* drho, double* vel)
     double* st = astage_out[k];
     DG_CUDA(cudaStreamWaitEvent(stream, out_free[k], 0));
     const GridMap g = grid_map(mesh);
-    const int threads = 256, blocks = 152 * 16;
+    const int threads = 128, blocks = 152 * 16;
     if (fp64())
         pack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((const double*)state_ptr(), mesh.fstride(),
                                                                        mesh.NP, g, drho ? st : nullptr,
