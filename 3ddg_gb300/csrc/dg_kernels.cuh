@@ -715,6 +715,26 @@ __global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int n
     }
 }
 
+// Host-order device staging -> state, walked in element order: the state
+// writes are contiguous per element and the scattered side is the read
+// (K-value runs along z), which costs less than partial-sector writes.  For
+// device memory only; pinned host memory is read by unpack_host_order_kernel.
+template <typename T>
+__global__ void unpack_elem_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g, int n_elem,
+                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize)
+{
+    const int K3 = g.K * g.K * g.K;
+    const size_t total = (size_t)n_elem * np;
+    for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < total; s += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(s / np), n = (int)(s % np);
+        if (n >= K3) continue;
+        const size_t i = grid_index(g, e, n);
+        state[s] = (T)rho[i];
+#pragma unroll
+        for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + s] = (T)vel[a * gsize + i];
+    }
+}
+
 template <typename T>
 __global__ void pack_grid_kernel(const T* __restrict__ state, size_t fs, int np, int nfields,
                                  GridMap g, int n_elem, double* __restrict__ out, size_t gsize)

@@ -465,11 +465,10 @@ int Solver::pack_out(const void* src, double* drho, double* vel)
 
 int Solver::unpack_in(const double* drho, const double* vel)
 {
-    const GridMap g = grid_map(mesh);
-    const int threads = 128, blocks = 152 * 16;
     const double* rho_d = (const double*)device_view(drho);
     const double* vel_d = (const double*)device_view(vel);
-    if (!rho_d || !vel_d) {
+    const bool staged = !rho_d || !vel_d;
+    if (staged) {
         int rc = ensure_staging();
         if (rc) return rc;
         DG_CUDA(cudaMemcpyAsync(staging, drho, gsize() * sizeof(double), cudaMemcpyHostToDevice, stream));
@@ -477,17 +476,36 @@ int Solver::unpack_in(const double* drho, const double* vel)
         rho_d = staging;
         vel_d = staging + gsize();
     }
-    if (fp64())
-        unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
-                                                                         mesh.NP, g, rho_d, vel_d, gsize());
-    else {
-        unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                        g, rho_d, vel_d, gsize());
-        DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
+    int rc = launch_unpack(rho_d, vel_d, staged);
+    if (rc) return rc;
+    DG_CUDA(cudaStreamSynchronize(stream));
+    return DG_OK;
+}
+
+// Host-order arrays -> state on the compute stream: device staging is walked in
+// element order, pinned host memory (read over the CPU-GPU link) in host order.
+int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_device)
+{
+    const GridMap g = grid_map(mesh);
+    const int threads = 128, blocks = 152 * 16;
+    if (on_device) {
+        if (fp64())
+            unpack_elem_order_kernel<double><<<blocks, 256, 0, stream>>>((double*)state_ptr(), mesh.fstride(), mesh.NP,
+                                                                         g, mesh.n_elem, rho_d, vel_d, gsize());
+        else
+            unpack_elem_order_kernel<float><<<blocks, 256, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
+                                                                        g, mesh.n_elem, rho_d, vel_d, gsize());
+    } else {
+        if (fp64())
+            unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
+                                                                             mesh.NP, g, rho_d, vel_d, gsize());
+        else
+            unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(),
+                                                                            mesh.NP, g, rho_d, vel_d, gsize());
     }
     launches++;
     DG_CUDA(cudaGetLastError());
-    DG_CUDA(cudaStreamSynchronize(stream));
+    if (!fp64()) DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
     ic_live = false;
     return DG_OK;
 }
@@ -523,20 +541,9 @@ int Solver::set_state_async(const double* drho, const double* vel)
     DG_CUDA(cudaMemcpyAsync(st + n, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, copy_in));
     DG_CUDA(cudaEventRecord(in_ready[k], copy_in));
     DG_CUDA(cudaStreamWaitEvent(stream, in_ready[k], 0));
-    const GridMap g = grid_map(mesh);
-    const int threads = 128, blocks = 152 * 16;
-    if (fp64()) {
-        unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
-                                                                         mesh.NP, g, st, st + n, n);
-    } else {
-        unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                        g, st, st + n, n);
-        DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
-    }
-    launches++;
-    DG_CUDA(cudaGetLastError());
+    rc = launch_unpack(st, st + n, true);
+    if (rc) return rc;
     DG_CUDA(cudaEventRecord(in_free[k], stream));
-    ic_live = false;
     return DG_OK;
 }
 

@@ -79,6 +79,7 @@ struct Solver {
     int ensure_staging();
     int pack_out(const void* src, double* drho, double* vel);
     int unpack_in(const double* drho, const double* vel);
+    int launch_unpack(const double* rho_d, const double* vel_d, bool on_device);
 
     // Asynchronous host transfers (dg_set_state_async / dg_get_state_async):
     // copy-engine streams and double-buffered device staging, so that one
