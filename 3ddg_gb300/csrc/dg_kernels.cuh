@@ -317,25 +317,62 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     }
 }
 
+// Face nodes of an element, numbered t = (2 a + side) K^2 + fi for the faces
+// -X +X -Y +Y -Z +Z, fi = c[(a+1)%3] K + c[(a+2)%3]: the element's node on
+// the face (nf) and the neighbour's node across it (nn, in the neighbour).
+template <int K>
+struct FaceNode {
+    int a, side, fi, nf, nn;
+    __device__ __forceinline__ explicit FaceNode(int t)
+    {
+        constexpr int K2 = K * K;
+        a = t / (2 * K2);
+        side = (t / K2) & 1;
+        fi = t % K2;
+        const int p = side ? K - 1 : 0;
+        nf = a == 0 ? p * K2 + fi : (a == 1 ? (fi % K) * K2 + p * K + fi / K : fi * K + p);
+        nn = nf + (side ? -(K - 1) : (K - 1)) * axis_stride<K>(a);
+    }
+};
+
+// Shared memory of the plain stage kernel: the line-sum operands (f, g as in
+// StageSmem) and each node's own mass flux and gradient, which the face phase
+// reads.
+template <typename T, int K>
+struct PlainSmem {
+    typename Pair<T>::type f[3][npt_of(K)];
+    typename Pair<T>::type g[3][2][K * K];
+    T m[3][npt_of(K)];
+    T q[3][npt_of(K)];
+};
+
 // ---------------------------------------------------------------------------
 // One RK stage of the plain (FP64) form: R = L(stage input), then the stage
 // combination dst = R' + s (cb - ca sigma) + cc old.
+//
+// The FP64 pipe is the bound, so the face fluxes are assigned densely: thread
+// n of an element evaluates face nodes n, n + NPT, ... of its 6 K^2, reading
+// the element's own values from shared memory.  (A thread per node evaluating
+// its own faces would issue every axis's face arithmetic in nearly every warp,
+// since almost every warp holds some node on each face pair.)  The
+// neighbour values of those face nodes are loaded with the thread's own node.
 // ---------------------------------------------------------------------------
 template <typename T, int K, bool DIFF>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
-    constexpr int K2 = K * K, K3 = K * K * K;
-    __shared__ StageSmem<T, K> sm_all[epb_of(K)];
-    StageSmem<T, K>& S = sm_all[threadIdx.y];
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
+    __shared__ PlainSmem<T, K> sm_all[epb_of(K)];
+    PlainSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
     const int e = blockIdx.x * epb_of(K) + threadIdx.y;
-    const bool act = n < K3 && e < m.n_elem;
+    const bool live = e < m.n_elem;
+    const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const size_t off = (size_t)e * io.np + n;
-    OpRows<T, K> R;
-    R.load(C, c, act);
+    OpRows<T, K> R_;
+    R_.load(C, c, act);
 
     T rho = T(0), u[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     if (act) {
@@ -346,6 +383,25 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
     }
+    // Neighbour (or exterior) values of this thread's face nodes.
+    T ro[R], uo[R], qo[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        ro[r] = uo[r] = qo[r] = T(0);
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        if (code >= 0) {
+            const size_t o2 = (size_t)code * io.np + F.nn;
+            ro[r] = load_in<false>(io, 0, o2);
+            uo[r] = load_in<false>(io, 1 + F.a, o2);
+            if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
+        } else {
+            exterior<T, K>(m, C, -1 - code, F.side, F.fi, ro[r], uo[r]);
+        }
+    }
+
     T fmom = T(0), fmass[3] = {T(0), T(0), T(0)};
     if (do_adv) {
         fmom = momentum_flux(rho, C.k1, C.k2);
@@ -356,41 +412,31 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     for (int a = 0; a < 3; a++) {
         S.f[a][n].x = fmom;
         S.f[a][n].y = DIFF ? fmass[a] + q[a] : fmass[a];
+        S.m[a][n] = fmass[a];
+        if (DIFF) S.q[a][n] = q[a];
     }
+    __syncthreads();
 
-    // Face terms: the thread owning a face node evaluates that face's numerical
-    // flux for its line (impedance upwind for advection, central for LDG),
-    // already multiplied by its lift scale.
-    if (act) {
+    // Face terms: the numerical flux (impedance upwind for advection, central
+    // for LDG) times its lift scale.
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (c[a] != 0 && c[a] != K - 1) continue;
-            const int side = c[a] == 0 ? 0 : 1;
-            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-            const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * a + side);
-            T ro, uo, qo = T(0);
-            if (code >= 0) {
-                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                const size_t o2 = (size_t)code * io.np + nn;
-                ro = load_in<false>(io, 0, o2);
-                uo = load_in<false>(io, 1 + a, o2);
-                if (DIFF) qo = __ldg(io.q + (size_t)a * io.fs + o2);
-            } else {
-                exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
-            }
-            T gm = T(0), gr = T(0);
-            if (do_adv) {
-                const T fmo = momentum_flux(ro, C.k1, C.k2);
-                const T fao = mass_flux(uo, ro, C.r0, C.linear_mass);
-                const T* cm = C.cM[a][side];
-                const T* cr = C.cA[a][side];
-                gm = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
-                gr = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3];
-            }
-            if (DIFF) gr += C.cQ[a][side] * (qo + q[a]);
-            S.g[a][side][fi].x = gm;
-            S.g[a][side][fi].y = gr;
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
+        T gm = T(0), gr = T(0);
+        if (do_adv) {
+            const T fmo = momentum_flux(ro[r], C.k1, C.k2);
+            const T fao = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
+            const T* cm = C.cM[F.a][F.side];
+            const T* cr = C.cA[F.a][F.side];
+            gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
+            gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
         }
+        if (DIFF) gr += C.cQ[F.a][F.side] * (qo[r] + S.q[F.a][F.nf]);
+        S.g[F.a][F.side][F.fi].x = gm;
+        S.g[F.a][F.side][F.fi].y = gr;
     }
     __syncthreads();
     if (!act) return;
@@ -398,21 +444,20 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
+        const int st = axis_stride<K>(a), base = n - c[a] * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
         const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-        T sm = R.l0[a] * g0.x, sr = R.l0[a] * g0.y;
-        sm += R.ln[a] * gN.x;
-        sr += R.ln[a] * gN.y;
+        T sm = R_.l0[a] * g0.x, sr = R_.l0[a] * g0.y;
+        sm += R_.ln[a] * gN.x;
+        sr += R_.ln[a] * gN.y;
 #pragma unroll
         for (int j = 0; j < K; j++) {
             const typename Pair<T>::type v = S.f[a][base + j * st];
-            sm += R.d[a][j] * v.x;
-            sr += R.d[a][j] * v.y;
+            sm += R_.d[a][j] * v.x;
+            sr += R_.d[a][j] * v.y;
         }
         r_rho += sr;
         r_u[a] = do_adv ? sm : T(0);
-        (void)ia;
     }
     const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);
 
