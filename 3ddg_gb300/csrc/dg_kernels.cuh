@@ -191,6 +191,24 @@ __device__ __forceinline__ int axis_stride(int a)
     return a == 0 ? K * K : (a == 1 ? K : 1);
 }
 
+// Face nodes of an element, numbered t = (2 a + side) K^2 + fi for the faces
+// -X +X -Y +Y -Z +Z, fi = c[(a+1)%3] K + c[(a+2)%3]: the element's node on
+// the face (nf) and the neighbour's node across it (nn, in the neighbour).
+template <int K>
+struct FaceNode {
+    int a, side, fi, nf, nn;
+    __device__ __forceinline__ explicit FaceNode(int t)
+    {
+        constexpr int K2 = K * K;
+        a = t / (2 * K2);
+        side = (t / K2) & 1;
+        fi = t % K2;
+        const int p = side ? K - 1 : 0;
+        nf = a == 0 ? p * K2 + fi : (a == 1 ? (fi % K) * K2 + p * K + fi / K : fi * K + p);
+        nn = nf + (side ? -(K - 1) : (K - 1)) * axis_stride<K>(a);
+    }
+};
+
 // ---------------------------------------------------------------------------
 // LDG gradient, stored as G_a = -D_c Q_a = (D_c / w_a)(D drho + M^-1 e_0 F_0 +
 // M^-1 e_N F_N) with the central flux F_0 = (drho_o[N] + drho_s[0]) / 2,
@@ -235,70 +253,53 @@ template <typename T, int K, bool INCR>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K), (grad_min_blocks<T, K>()))
 ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp)
 {
-    constexpr int K2 = K * K, K3 = K * K * K;
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
     __shared__ GradSmem<T, K> sm_all[epb_of(K)];
     GradSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
     const int e = blockIdx.x * epb_of(K) + threadIdx.y;
-    const bool act = n < K3 && e < m.n_elem;
+    const bool live = e < m.n_elem;
+    const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
-    OpRows<T, K> R;
+    // Face nodes assigned densely (see stage_kernel): their neighbour (or
+    // exterior) values are loaded with the thread's own node.
+    int code[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        code[r] = 0;
+        if (live && t < NF) {
+            const FaceNode<K> F(t);
+            code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        }
+    }
     T rho = T(0);
-    if constexpr (INCR) {
-        // FP32 (latency-bound): face-table codes first, so that the neighbour
-        // loads that depend on them are issued together with the own load.
-        int code[3] = {0, 0, 0};
+    if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
+    T ro[R];
 #pragma unroll
-        for (int a = 0; a < 3; a++)
-            if (act && (c[a] == 0 || c[a] == K - 1))
-                code[a] = __ldg(m.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
-        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
-        T ro[3] = {T(0), T(0), T(0)};
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
-            const int side = c[a] == 0 ? 0 : 1;
-            if (code[a] >= 0) {
-                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                ro[a] = load_in<INCR>(io, 0, (size_t)code[a] * io.np + nn);
-            } else {
-                T uo;
-                exterior<T, K>(m, C, -1 - code[a], side, c[(a + 1) % 3] * K + c[(a + 2) % 3], ro[a], uo);
-            }
+    for (int r = 0; r < R; r++) {
+        ro[r] = T(0);
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        if (code[r] >= 0) {
+            ro[r] = load_in<INCR>(io, 0, (size_t)code[r] * io.np + F.nn);
+        } else {
+            T uo;
+            exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo);
         }
-        R.load(C, c, act);
-        S.r[n] = rho;
-        if (act) {
+    }
+    OpRows<T, K> R_;
+    R_.load(C, c, act);
+    S.r[n] = rho;
+    __syncthreads();
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                if (c[a] != 0 && c[a] != K - 1) continue;
-                const int side = c[a] == 0 ? 0 : 1;
-                S.fl[a][side][c[(a + 1) % 3] * K + c[(a + 2) % 3]] = C.cQ[a][side] * (ro[a] + rho);
-            }
-        }
-    } else {
-        // FP64 (bound by the FP64 pipe): loads in program order.
-        R.load(C, c, act);
-        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
-        S.r[n] = rho;
-        if (act) {
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                if (c[a] != 0 && c[a] != K - 1) continue;
-                const int side = c[a] == 0 ? 0 : 1;
-                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * a + side);
-                T ro, uo;
-                if (code >= 0) {
-                    const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                    ro = load_in<INCR>(io, 0, (size_t)code * io.np + nn);
-                } else {
-                    exterior<T, K>(m, C, -1 - code, side, fi, ro, uo);
-                }
-                S.fl[a][side][fi] = C.cQ[a][side] * (ro + rho);
-            }
-        }
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        S.fl[F.a][F.side][F.fi] = C.cQ[F.a][F.side] * (ro[r] + S.r[F.nf]);
     }
     __syncthreads();
     if (!act) return;
@@ -308,32 +309,14 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         const int ia = c[a];
         const int base = n - ia * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T s = R.l0[a] * S.fl[a][0][fi];
-        s += R.ln[a] * S.fl[a][1][fi];
+        T s = R_.l0[a] * S.fl[a][0][fi];
+        s += R_.ln[a] * S.fl[a][1][fi];
 #pragma unroll
-        for (int j = 0; j < K; j++) s += R.d[a][j] * S.r[base + j * st];
+        for (int j = 0; j < K; j++) s += R_.d[a][j] * S.r[base + j * st];
         io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
         (void)ia;
     }
 }
-
-// Face nodes of an element, numbered t = (2 a + side) K^2 + fi for the faces
-// -X +X -Y +Y -Z +Z, fi = c[(a+1)%3] K + c[(a+2)%3]: the element's node on
-// the face (nf) and the neighbour's node across it (nn, in the neighbour).
-template <int K>
-struct FaceNode {
-    int a, side, fi, nf, nn;
-    __device__ __forceinline__ explicit FaceNode(int t)
-    {
-        constexpr int K2 = K * K;
-        a = t / (2 * K2);
-        side = (t / K2) & 1;
-        fi = t % K2;
-        const int p = side ? K - 1 : 0;
-        nf = a == 0 ? p * K2 + fi : (a == 1 ? (fi % K) * K2 + p * K + fi / K : fi * K + p);
-        nn = nf + (side ? -(K - 1) : (K - 1)) * axis_stride<K>(a);
-    }
-};
 
 // Shared memory of the plain stage kernel: the line-sum operands (f, g as in
 // StageSmem) and each node's own mass flux and gradient, which the face phase
@@ -474,34 +457,38 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 }
 
 // ---------------------------------------------------------------------------
-// One RK stage of the increment (FP32) form, arranged so that every global
-// load a thread makes is issued before the first value is used: the
-// neighbour codes and sigma, the thread's own u, d, gradient and Kahan
-// compensation, and then the neighbour values across its faces.  The kernel
-// waits on memory latency, so the loads wait together instead of in four
-// dependent waves (own state, face table, neighbour values, reloads of u and
-// d for the update).
+// One RK stage of the increment (FP32) form.  The kernel waits on memory
+// latency and on the L1 data pipe, so every global load a thread makes is
+// issued before the first value is used (face-table codes and sigma, its own
+// u, d, gradient and Kahan compensation, the neighbour values of its face
+// nodes), and the face nodes are assigned densely as in stage_kernel, which
+// also makes the neighbour gathers denser warp requests.  The face fluxes are
+// evaluated after a barrier from the element's own values in shared memory.
 // ---------------------------------------------------------------------------
 template <typename T, int K, bool DIFF>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
 incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
-    constexpr int K2 = K * K, K3 = K * K * K;
-    __shared__ StageSmem<T, K> sm_all[epb_of(K)];
-    StageSmem<T, K>& S = sm_all[threadIdx.y];
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
+    __shared__ PlainSmem<T, K> sm_all[epb_of(K)];
+    PlainSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
     const int e = blockIdx.x * epb_of(K) + threadIdx.y;
-    const bool act = n < K3 && e < m.n_elem;
+    const bool live = e < m.n_elem;
+    const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const size_t off = (size_t)e * io.np + n;
 
-    bool on[3];
-    int code[3] = {0, 0, 0};
+    int code[R];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        on[a] = act && (c[a] == 0 || c[a] == K - 1);
-        if (on[a]) code[a] = __ldg(m.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        code[r] = 0;
+        if (live && t < NF) {
+            const FaceNode<K> F(t);
+            code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        }
     }
     const T sig = (act && do_sponge) ? __ldg(m.sigma + e) : T(0);
     T ub[4] = {T(0), T(0), T(0), T(0)}, dv[4] = {T(0), T(0), T(0), T(0)};
@@ -517,25 +504,24 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
     }
-    OpRows<T, K> R;
-    R.load(C, c, act);
-
-    T ro[3], uo[3], qo[3];
+    T ro[R], uo[R], qo[R];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        ro[a] = uo[a] = qo[a] = T(0);
-        if (!on[a]) continue;
-        const int side = c[a] == 0 ? 0 : 1;
-        if (code[a] >= 0) {
-            const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-            const size_t o2 = (size_t)code[a] * io.np + nn;
-            ro[a] = load_in<true>(io, 0, o2);
-            uo[a] = load_in<true>(io, 1 + a, o2);
-            if (DIFF) qo[a] = __ldg(io.q + (size_t)a * io.fs + o2);
+    for (int r = 0; r < R; r++) {
+        ro[r] = uo[r] = qo[r] = T(0);
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        if (code[r] >= 0) {
+            const size_t o2 = (size_t)code[r] * io.np + F.nn;
+            ro[r] = load_in<true>(io, 0, o2);
+            uo[r] = load_in<true>(io, 1 + F.a, o2);
+            if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
         } else {
-            exterior<T, K>(m, C, -1 - code[a], side, c[(a + 1) % 3] * K + c[(a + 2) % 3], ro[a], uo[a]);
+            exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo[r]);
         }
     }
+    OpRows<T, K> R_;
+    R_.load(C, c, act);
 
     const T rho = ub[0] + dv[0];
     const T u[3] = {ub[1] + dv[1], ub[2] + dv[2], ub[3] + dv[3]};
@@ -549,24 +535,28 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
     for (int a = 0; a < 3; a++) {
         S.f[a][n].x = fmom;
         S.f[a][n].y = DIFF ? fmass[a] + q[a] : fmass[a];
+        S.m[a][n] = fmass[a];
+        if (DIFF) S.q[a][n] = q[a];
     }
+    __syncthreads();
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        if (!on[a]) continue;
-        const int side = c[a] == 0 ? 0 : 1;
-        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        if (!live || t >= NF) continue;
+        const FaceNode<K> F(t);
+        const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
         T gm = T(0), gr = T(0);
         if (do_adv) {
-            const T fmo = momentum_flux(ro[a], C.k1, C.k2);
-            const T fao = mass_flux(uo[a], ro[a], C.r0, C.linear_mass);
-            const T* cm = C.cM[a][side];
-            const T* cr = C.cA[a][side];
-            gm = fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3];
-            gr = fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3];
+            const T fmo = momentum_flux(ro[r], C.k1, C.k2);
+            const T fao = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
+            const T* cm = C.cM[F.a][F.side];
+            const T* cr = C.cA[F.a][F.side];
+            gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
+            gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
         }
-        if (DIFF) gr += C.cQ[a][side] * (qo[a] + q[a]);
-        S.g[a][side][fi].x = gm;
-        S.g[a][side][fi].y = gr;
+        if (DIFF) gr += C.cQ[F.a][F.side] * (qo[r] + S.q[F.a][F.nf]);
+        S.g[F.a][F.side][F.fi].x = gm;
+        S.g[F.a][F.side][F.fi].y = gr;
     }
     __syncthreads();
     if (!act) return;
@@ -577,14 +567,14 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
         const int st = axis_stride<K>(a), base = n - c[a] * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
         const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-        T sm = R.l0[a] * g0.x, sr = R.l0[a] * g0.y;
-        sm += R.ln[a] * gN.x;
-        sr += R.ln[a] * gN.y;
+        T sm = R_.l0[a] * g0.x, sr = R_.l0[a] * g0.y;
+        sm += R_.ln[a] * gN.x;
+        sr += R_.ln[a] * gN.y;
 #pragma unroll
         for (int j = 0; j < K; j++) {
             const typename Pair<T>::type v = S.f[a][base + j * st];
-            sm += R.d[a][j] * v.x;
-            sr += R.d[a][j] * v.y;
+            sm += R_.d[a][j] * v.x;
+            sr += R_.d[a][j] * v.y;
         }
         r[0] += sr;
         r[1 + a] = do_adv ? sm : T(0);
