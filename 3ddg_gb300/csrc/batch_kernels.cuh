@@ -48,7 +48,8 @@ __device__ __forceinline__ float batch_in(const BatchProblem& P, const float* ub
 template <int K>
 __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
 {
-    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K2;
+    constexpr int R = (NF + NPT - 1) / NPT;
     GradSmem<float, K>* SM = reinterpret_cast<GradSmem<float, K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
     const int c[3] = {n / K2, (n / K) % K, n % K};
@@ -56,39 +57,45 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
         const int e = c0 + slot;
-        const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
+        const bool live = slot < EPB && e < T.e0 + T.count;
+        const bool act = live && n < K3;
         GradSmem<float, K>& S = SM[slot < EPB ? slot : 0];
-        // Face-table codes first, so that the neighbour loads that depend on
-        // them are issued together with the own load (the kernel waits on
-        // memory latency).
-        int code[3] = {0, 0, 0};
+        // Face nodes assigned densely (see stage_kernel); every global load
+        // is issued before the first use (the kernel waits on memory latency).
+        int code[R];
 #pragma unroll
-        for (int a = 0; a < 3; a++)
-            if (act && (c[a] == 0 || c[a] == K - 1))
-                code[a] = __ldg(P.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            code[r] = 0;
+            if (live && t < NF) {
+                const FaceNode<K> F(t);
+                code[r] = __ldg(P.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+            }
+        }
         float rho = 0.f;
         if (act) rho = batch_in<K>(P, ub, inc, 0, (size_t)e * P.np + n);
-        float ro[3] = {0.f, 0.f, 0.f};
+        float ro[R];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
-            const int side = c[a] == 0 ? 0 : 1;
-            if (code[a] >= 0) {
-                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                ro[a] = batch_in<K>(P, ub, inc, 0, (size_t)code[a] * P.np + nn);
+        for (int r = 0; r < R; r++) {
+            ro[r] = 0.f;
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            if (code[r] >= 0) {
+                ro[r] = batch_in<K>(P, ub, inc, 0, (size_t)code[r] * P.np + F.nn);
             } else {
                 float uo;
-                batch_exterior(P, -1 - code[a], stage, ro[a], uo);
+                batch_exterior(P, -1 - code[r], stage, ro[r], uo);
             }
         }
         if (slot < EPB) S.r[n] = rho;
-        if (act) {
+        __syncthreads();
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                if (c[a] != 0 && c[a] != K - 1) continue;
-                const int side = c[a] == 0 ? 0 : 1;
-                S.fl[a][side][c[(a + 1) % 3] * K + c[(a + 2) % 3]] = (side ? -0.5f : 0.5f) * (ro[a] + rho);
-            }
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            S.fl[F.a][F.side][F.fi] = (F.side ? -0.5f : 0.5f) * (ro[r] + S.r[F.nf]);
         }
         __syncthreads();
         if (act) {
@@ -110,8 +117,9 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
 template <int K>
 __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
 {
-    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
-    StageSmem<float, K>* SM = reinterpret_cast<StageSmem<float, K>*>(smraw);
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K2;
+    constexpr int R = (NF + NPT - 1) / NPT;
+    PlainSmem<float, K>* SM = reinterpret_cast<PlainSmem<float, K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const float* ub = P.u[P.cur];
@@ -121,17 +129,24 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
     const float ca = P.ca[stage], cb = P.cb[stage], eps = final_stage ? P.eps : 0.f;
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
         const int e = c0 + slot;
-        const bool act = slot < EPB && n < K3 && e < T.e0 + T.count;
-        StageSmem<float, K>& S = SM[slot < EPB ? slot : 0];
+        const bool live = slot < EPB && e < T.e0 + T.count;
+        const bool act = live && n < K3;
+        PlainSmem<float, K>& S = SM[slot < EPB ? slot : 0];
         const size_t off = (size_t)e * P.np + n;
         // Every global load before the first use (the kernel waits on memory
         // latency): face-table codes and sigma, the own u, d, gradient and
-        // compensation, then the neighbour values across the node's faces.
-        int code[3] = {0, 0, 0};
+        // compensation, then the neighbour values of the densely assigned
+        // face nodes (see stage_kernel).
+        int code[R];
 #pragma unroll
-        for (int a = 0; a < 3; a++)
-            if (act && (c[a] == 0 || c[a] == K - 1))
-                code[a] = __ldg(P.nbr + (size_t)e * 6 + 2 * a + (c[a] == 0 ? 0 : 1));
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            code[r] = 0;
+            if (live && t < NF) {
+                const FaceNode<K> F(t);
+                code[r] = __ldg(P.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+            }
+        }
         const float sig = act ? __ldg(P.sigma + e) : 0.f;
         float ubv[4] = {0.f, 0.f, 0.f, 0.f}, dv[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
         float q[3] = {0.f, 0.f, 0.f};
@@ -145,19 +160,20 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(P.q + (size_t)a * P.fs + off);
         }
-        float ro[3] = {0.f, 0.f, 0.f}, uo[3] = {0.f, 0.f, 0.f}, qo[3] = {0.f, 0.f, 0.f};
+        float ro[R], uo[R], qo[R];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (!act || (c[a] != 0 && c[a] != K - 1)) continue;
-            const int side = c[a] == 0 ? 0 : 1;
-            if (code[a] >= 0) {
-                const int nn = n + ((side ? 0 : K - 1) - c[a]) * axis_stride<K>(a);
-                const size_t o2 = (size_t)code[a] * P.np + nn;
-                ro[a] = batch_in<K>(P, ub, inc, 0, o2);
-                uo[a] = batch_in<K>(P, ub, inc, 1 + a, o2);
-                qo[a] = __ldg(P.q + (size_t)a * P.fs + o2);
+        for (int r = 0; r < R; r++) {
+            ro[r] = uo[r] = qo[r] = 0.f;
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            if (code[r] >= 0) {
+                const size_t o2 = (size_t)code[r] * P.np + F.nn;
+                ro[r] = batch_in<K>(P, ub, inc, 0, o2);
+                uo[r] = batch_in<K>(P, ub, inc, 1 + F.a, o2);
+                qo[r] = __ldg(P.q + (size_t)F.a * P.fs + o2);
             } else {
-                batch_exterior(P, -1 - code[a], stage, ro[a], uo[a]);
+                batch_exterior(P, -1 - code[r], stage, ro[r], uo[r]);
             }
         }
         const float rho = ubv[0] + dv[0];
@@ -168,22 +184,26 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
         for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, P.r0, P.linear_mass);
         if (slot < EPB) {
 #pragma unroll
-            for (int a = 0; a < 3; a++) S.f[a][n] = make_float2(fmom, fmass[a] + q[a]);
-        }
-        if (act) {
-#pragma unroll
             for (int a = 0; a < 3; a++) {
-                if (c[a] != 0 && c[a] != K - 1) continue;
-                const int side = c[a] == 0 ? 0 : 1;
-                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                const float fmo = momentum_flux(ro[a], P.k1, P.k2);
-                const float fao = mass_flux(uo[a], ro[a], P.r0, P.linear_mass);
-                const float* cm = P.cM[side];
-                const float* cr = P.cA[side];
-                S.g[a][side][fi] = make_float2(fmo * cm[0] + fmom * cm[1] + fao * cm[2] + fmass[a] * cm[3],
-                                               fmo * cr[0] + fmom * cr[1] + fao * cr[2] + fmass[a] * cr[3] +
-                                                   (side ? -0.5f : 0.5f) * (qo[a] + q[a]));
+                S.f[a][n] = make_float2(fmom, fmass[a] + q[a]);
+                S.m[a][n] = fmass[a];
+                S.q[a][n] = q[a];
             }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            const float fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
+            const float fmo = momentum_flux(ro[r], P.k1, P.k2);
+            const float fao = mass_flux(uo[r], ro[r], P.r0, P.linear_mass);
+            const float* cm = P.cM[F.side];
+            const float* cr = P.cA[F.side];
+            S.g[F.a][F.side][F.fi] = make_float2(fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3],
+                                                 fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3] +
+                                                     (F.side ? -0.5f : 0.5f) * (qo[r] + S.q[F.a][F.nf]));
         }
         __syncthreads();
         if (act) {
@@ -232,9 +252,9 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
 __host__ __device__ constexpr size_t batch_smem_bytes()
 {
     size_t m = 0;
-    const size_t s2 = bepb_of(2) * sizeof(StageSmem<float, 2>), s3 = bepb_of(3) * sizeof(StageSmem<float, 3>);
-    const size_t s4 = bepb_of(4) * sizeof(StageSmem<float, 4>), s5 = bepb_of(5) * sizeof(StageSmem<float, 5>);
-    const size_t s6 = bepb_of(6) * sizeof(StageSmem<float, 6>);
+    const size_t s2 = bepb_of(2) * sizeof(PlainSmem<float, 2>), s3 = bepb_of(3) * sizeof(PlainSmem<float, 3>);
+    const size_t s4 = bepb_of(4) * sizeof(PlainSmem<float, 4>), s5 = bepb_of(5) * sizeof(PlainSmem<float, 5>);
+    const size_t s6 = bepb_of(6) * sizeof(PlainSmem<float, 6>);
     m = s2 > m ? s2 : m;
     m = s3 > m ? s3 : m;
     m = s4 > m ? s4 : m;
