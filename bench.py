@@ -545,8 +545,6 @@ def run_reference(a, dist: Dist):
     W = importlib.import_module("3ddg_gb300.workloads")
     cfg = W.config2(seed=0)
     procs = os.cpu_count() or 1
-    per_step = []
-    sample = cpu_sample_cfg(cfg)
     # warm-up + timed steps of the sample, all host cores in parallel
     base = cpu_baseline(cfg, procs, seconds=max(2.0, 0.5 * (a.steps + a.warmup)), max_steps=a.steps)
     value = base["value"]
@@ -560,7 +558,6 @@ def run_reference(a, dist: Dist):
         "cpu_baseline": base,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    del per_step, sample
     return line
 
 
