@@ -48,9 +48,9 @@ void fill_ops(BatchProblem& P, const LineOperators& op, const dg_params& p)
         make_stage_const<double, K>(1.0, op.deriv.data(), op.lift0.data(), op.liftN.data(), w1, p.rho0, p.c0,
                                     p.b_over_a, p.diff_const);
     for (int i = 0; i < K; i++) {
-        for (int j = 0; j < K; j++) P.D[i][j] = (float)op.deriv[i * K + j];
-        P.L0[i] = (float)op.lift0[i];
-        P.LN[i] = (float)op.liftN[i];
+        for (int j = 0; j < K; j++) P.rows[i][j] = (float)op.deriv[i * K + j];
+        P.rows[i][K] = (float)op.lift0[i];
+        P.rows[i][K + 1] = (float)op.liftN[i];
     }
     for (int s = 0; s < 2; s++)
         for (int i = 0; i < 4; i++) {

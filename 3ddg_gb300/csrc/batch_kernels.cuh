@@ -45,6 +45,21 @@ __device__ __forceinline__ float batch_in(const BatchProblem& P, const float* ub
     return v;
 }
 
+// Row ia of the problem's operator (D row, then the two lift entries) from
+// the shared-memory descriptor into registers: two 16-byte loads.
+template <int K>
+__device__ __forceinline__ void batch_row(const BatchProblem& P, int ia, float d[K], float& l0, float& ln)
+{
+    float row[8];
+    const float4* src = reinterpret_cast<const float4*>(P.rows[ia]);
+    reinterpret_cast<float4*>(row)[0] = src[0];
+    reinterpret_cast<float4*>(row)[1] = src[1];
+#pragma unroll
+    for (int j = 0; j < K; j++) d[j] = row[j];
+    l0 = row[K];
+    ln = row[K + 1];
+}
+
 template <int K>
 __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
 {
@@ -103,10 +118,12 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
             for (int a = 0; a < 3; a++) {
                 const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
                 const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                float s = P.L0[ia] * S.fl[a][0][fi];
-                s += P.LN[ia] * S.fl[a][1][fi];
+                float d[K], l0, ln;
+                batch_row<K>(P, ia, d, l0, ln);
+                float s = l0 * S.fl[a][0][fi];
+                s += ln * S.fl[a][1][fi];
 #pragma unroll
-                for (int j = 0; j < K; j++) s += P.D[ia][j] * S.r[base + j * st];
+                for (int j = 0; j < K; j++) s += d[j] * S.r[base + j * st];
                 P.q[(size_t)a * P.fs + (size_t)e * P.np + n] = P.gscale[a] * s;
             }
         }
@@ -212,13 +229,15 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
             for (int a = 0; a < 3; a++) {
                 const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
                 const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+                float d[K], l0, ln;
+                batch_row<K>(P, ia, d, l0, ln);
                 const float2 g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-                float sm = P.L0[ia] * g0.x, sr = P.L0[ia] * g0.y;
-                sm += P.LN[ia] * gN.x;
-                sr += P.LN[ia] * gN.y;
+                float sm = l0 * g0.x, sr = l0 * g0.y;
+                sm += ln * gN.x;
+                sr += ln * gN.y;
 #pragma unroll
                 for (int j = 0; j < K; j++) {
-                    const float dj = P.D[ia][j];
+                    const float dj = d[j];
                     const float2 v = S.f[a][base + j * st];
                     sm += dj * v.x;
                     sr += dj * v.y;

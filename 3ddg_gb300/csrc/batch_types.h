@@ -19,8 +19,10 @@ struct BatchProblem {
     const int* nbr;        // n_elem x 6, problem-local; boundary: -1 - face
     const float* sigma;    // n_elem
     size_t fs;             // field stride n_elem * np
-    float D[BATCH_KMAX][BATCH_KMAX];
-    float L0[BATCH_KMAX], LN[BATCH_KMAX];
+    // rows[i] = (D[i][0..K-1], L0[i], LN[i], 0...): the unit-interval
+    // derivative row and the lift entries of node i, 16-byte aligned so a
+    // thread loads its row with two vector loads.
+    alignas(16) float rows[BATCH_KMAX][8];
     float invw[3];         // 1 / w_a
     float gscale[3];       // D_c / w_a
     float cM[2][4], cA[2][4];  // face coefficients with the lift scales, w factored out
