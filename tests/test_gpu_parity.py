@@ -235,3 +235,46 @@ def test_async_transfers_match_sync(precision, solver_for):
         a.set_state_async(np.zeros(shape), np.zeros((3,) + shape))
     with pytest.raises(m.DGError, match="page-locked"):
         a.state_async(np.zeros(shape), None)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_async_transfers_ordering(precision, solver_for):
+    """Downloads between steps without uploads (the step waits for the pack of
+    the buffer it writes), a download right after an upload, and synchronous
+    calls mixed in: every download holds the state at its place in the call
+    sequence."""
+    import torch
+    cfg = small(order=2, ne=(3, 3, 4))
+    cfg["PRECISION"] = precision
+    a, b = solver_for(cfg), solver_for(cfg)
+    shape = a.dims
+    rng = np.random.default_rng(5)
+
+    def pinned(shp):
+        return torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
+
+    r0, v0 = pinned(shape), pinned((3,) + shape)
+    r0[...] = rng.standard_normal(shape) * 1e-3
+    v0[...] = rng.standard_normal((3,) + shape) * 1e-6
+    outs = [(pinned(shape), pinned((3,) + shape)) for _ in range(5)]
+    a.set_state_async(r0, v0)
+    a.state_async(*outs[0])           # right after the upload
+    for k in range(1, 4):
+        a.step(cfg["DT"], 1)
+        a.state_async(*outs[k])       # no upload in between
+    r_sync, v_sync = a.state()        # synchronous read in the mix
+    a.set_state(r_sync, v_sync)       # synchronous write after an async download
+    a.step(cfg["DT"], 1)
+    a.state_async(*outs[4])
+    a.synchronize()
+    b.set_state(r0, v0)
+    exp = [b.state()]
+    for k in range(1, 4):
+        b.step(cfg["DT"], 1)
+        exp.append(b.state())
+    b.set_state(*exp[3])  # as a does (in FP32 this also clears the Kahan compensation)
+    b.step(cfg["DT"], 1)
+    exp.append(b.state())
+    for k in range(5):
+        assert np.array_equal(outs[k][0], exp[k][0]) and np.array_equal(outs[k][1], exp[k][1]), k
+    assert np.array_equal(r_sync, exp[3][0])
