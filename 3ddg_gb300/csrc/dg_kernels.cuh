@@ -156,6 +156,7 @@ template <typename T, int K>
 struct GradSmem {
     T r[npt_of(K)];
     T fl[3][2][K * K];
+    T out[3][npt_of(K)];  // line-owner results (FP32, K >= 5)
 };
 
 template <bool INCR, typename T>
@@ -251,9 +252,12 @@ __host__ __device__ constexpr int grad_min_blocks()
 
 template <typename T, int K, bool INCR>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K), (grad_min_blocks<T, K>()))
-ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp)
+ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, const OpConst<T, K> Cv)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
+    // FP32 (bound by the L1 data pipe) with K >= 5: line owners, as in
+    // incr_stage_kernel; FP64 (bound by the FP64 pipe) keeps per-node sums.
+    constexpr bool LINES = INCR && K >= 5;
     __shared__ GradSmem<T, K> sm_all[epb_of(K)];
     GradSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
@@ -291,7 +295,7 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         }
     }
     OpRows<T, K> R_;
-    R_.load(C, c, act);
+    if constexpr (!LINES) R_.load(C, c, act);
     S.r[n] = rho;
     __syncthreads();
 #pragma unroll
@@ -302,6 +306,32 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         S.fl[F.a][F.side][F.fi] = C.cQ[F.a][F.side] * (ro[r] + S.r[F.nf]);
     }
     __syncthreads();
+    if constexpr (LINES) {
+        constexpr int WPA = (K2 + 31) / 32;
+        const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
+        if (live && a < 3 && t < K2) {
+            const int st = axis_stride<K>(a);
+            const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
+            T v[K];
+#pragma unroll
+            for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+            const T f0 = S.fl[a][0][t], fN = S.fl[a][1][t];
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                const T* row = Cv.rows[a][i];
+                T s2 = row[K] * f0;
+                s2 += row[K + 1] * fN;
+#pragma unroll
+                for (int j = 0; j < K; j++) s2 += row[j] * v[j];
+                S.out[a][b0 + i * st] = s2;
+            }
+        }
+        __syncthreads();
+        if (!act) return;
+#pragma unroll
+        for (int a2 = 0; a2 < 3; a2++) io.q_out[(size_t)a2 * io.fs + (size_t)e * io.np + n] = S.out[a2][n];
+        return;
+    }
     if (!act) return;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -464,11 +494,21 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 // nodes), and the face nodes are assigned densely as in stage_kernel, which
 // also makes the neighbour gathers denser warp requests.  The face fluxes are
 // evaluated after a barrier from the element's own values in shared memory.
+//
+// The line sums (the L1 data pipe's largest load: 2 (K + 2) shared-memory
+// operands per node and axis when each node sums its own lines) are done by
+// line owners for K >= 5: warps take one axis each, a lane one line of the
+// element, reads the line's K flux pairs and two face terms once and produces
+// all K outputs, with the operator rows taken from kernel-parameter space
+// (``Cv``; warp-uniform indices, so constant-bank operands).  The per-axis
+// results go to shared memory and each node thread adds them up.
 // ---------------------------------------------------------------------------
 template <typename T, int K, bool DIFF>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K))
-incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
+incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, const OpConst<T, K> Cv,
+                  int do_adv, int do_sponge)
 {
+    constexpr bool LINES = K >= 5;  // three warp-groups of ceil(K^2 / 32) warps fit in NPT
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
     __shared__ PlainSmem<T, K> sm_all[epb_of(K)];
     PlainSmem<T, K>& S = sm_all[threadIdx.y];
@@ -521,7 +561,7 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
         }
     }
     OpRows<T, K> R_;
-    R_.load(C, c, act);
+    if constexpr (!LINES) R_.load(C, c, act);
 
     const T rho = ub[0] + dv[0];
     const T u[3] = {ub[1] + dv[1], ub[2] + dv[2], ub[3] + dv[3]};
@@ -559,25 +599,61 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
         S.g[F.a][F.side][F.fi].y = gr;
     }
     __syncthreads();
-    if (!act) return;
 
     T r[4] = {T(0), T(0), T(0), T(0)};
+    if constexpr (LINES) {
+        // Line owners; the per-axis results reuse S.m (density) and S.q
+        // (momentum), whose last readers were the face terms before the barrier.
+        constexpr int WPA = (K2 + 31) / 32;
+        const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
+        if (live && a < 3 && t < K2) {
+            const int st = axis_stride<K>(a);
+            const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
+            typename Pair<T>::type v[K];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int st = axis_stride<K>(a), base = n - c[a] * st;
-        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-        T sm = R_.l0[a] * g0.x, sr = R_.l0[a] * g0.y;
-        sm += R_.ln[a] * gN.x;
-        sr += R_.ln[a] * gN.y;
+            for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st];
+            const typename Pair<T>::type g0 = S.g[a][0][t], gN = S.g[a][1][t];
 #pragma unroll
-        for (int j = 0; j < K; j++) {
-            const typename Pair<T>::type v = S.f[a][base + j * st];
-            sm += R_.d[a][j] * v.x;
-            sr += R_.d[a][j] * v.y;
+            for (int i = 0; i < K; i++) {
+                const T* row = Cv.rows[a][i];
+                T sm = row[K] * g0.x, sr = row[K] * g0.y;
+                sm += row[K + 1] * gN.x;
+                sr += row[K + 1] * gN.y;
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    sm += row[j] * v[j].x;
+                    sr += row[j] * v[j].y;
+                }
+                S.m[a][b0 + i * st] = sr;
+                S.q[a][b0 + i * st] = sm;
+            }
         }
-        r[0] += sr;
-        r[1 + a] = do_adv ? sm : T(0);
+        __syncthreads();
+        if (!act) return;
+#pragma unroll
+        for (int a2 = 0; a2 < 3; a2++) {
+            r[0] += S.m[a2][n];
+            r[1 + a2] = do_adv ? S.q[a2][n] : T(0);
+        }
+    } else {
+        if (!act) return;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int st = axis_stride<K>(a), base = n - c[a] * st;
+            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+            const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
+            T sm = R_.l0[a] * g0.x, sr = R_.l0[a] * g0.y;
+            sm += R_.ln[a] * gN.x;
+            sr += R_.ln[a] * gN.y;
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                const typename Pair<T>::type v = S.f[a][base + j * st];
+                sm += R_.d[a][j] * v.x;
+                sr += R_.d[a][j] * v.y;
+            }
+            r[0] += sr;
+            r[1 + a] = do_adv ? sm : T(0);
+        }
     }
     const T ks = io.ca * sig;
     const T cbe = io.cb - ks, ce = io.eps - ks;

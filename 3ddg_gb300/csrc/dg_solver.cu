@@ -115,8 +115,15 @@ int upload_consts_k(Solver& s, double dt)
     // stream-ordered after every launch that used the previous operators
     cudaError_t e = cudaMemcpyAsync(s.d_const, h.data(), 5 * slot, cudaMemcpyHostToDevice, s.stream);
     if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    s.h_const = std::move(h);
     s.const_dt = dt;
     return DG_OK;
+}
+
+template <typename T, int K>
+const OpConst<T, K>& host_const(const Solver& s, int slot)
+{
+    return *(const OpConst<T, K>*)(s.h_const.data() + (size_t)slot * const_slot<T, K>());
 }
 
 template <typename T, int K>
@@ -132,7 +139,7 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(1, &ev);
-    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, const_ptr<T, K>(s, 3));
+    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, const_ptr<T, K>(s, 3), host_const<T, K>(s, 3));
     s.prof_end(1, ev, grad_bytes(s, io), grad_flops(s));
     s.launches++;
 }
@@ -146,10 +153,13 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slo
     cudaEvent_t ev = nullptr;
     s.prof_begin(0, &ev);
     if constexpr (INCR) {
+        const OpConst<T, K>& Cv = host_const<T, K>(s, slot);
         if (s.p.eval_diff)
-            incr_stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+            incr_stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, Cv, s.p.eval_advect,
+                                                                       s.p.eval_sponge);
         else
-            incr_stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+            incr_stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, Cv, s.p.eval_advect,
+                                                                        s.p.eval_sponge);
     } else {
         if (s.p.eval_diff)
             stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);

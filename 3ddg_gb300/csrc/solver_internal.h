@@ -36,6 +36,7 @@ struct Solver {
     void* d_bnd_ap = nullptr;
     int* d_bnd_src = nullptr;
     void* d_const = nullptr;  // per-launch operators: 3 RK stages, LDG gradient, bare RHS
+    std::vector<char> h_const;  // host copy of d_const (for by-value kernel parameters)
     double const_dt = 0.0;
     int cur = 0;
     bool ic_live = false;

@@ -278,3 +278,19 @@ def test_async_transfers_ordering(precision, solver_for):
     for k in range(5):
         assert np.array_equal(outs[k][0], exp[k][0]) and np.array_equal(outs[k][1], exp[k][1]), k
     assert np.array_equal(r_sync, exp[3][0])
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5, 6, 7])
+def test_fp32_every_order_within_tolerance(order, solver_for):
+    """FP32 form (per-node line sums for K <= 4, line owners above) against the
+    FP64 path on the same inputs: relative L2 pressure error <= 1e-5."""
+    cfg = small(order=order, ne=(4, 3, 4))
+    s64 = solver_for(cfg)
+    s32 = solver_for(dict(cfg, PRECISION=32))
+    for s in (s64, s32):
+        s.step(cfg["DT"], 10)
+    r64, v64 = s64.state()
+    r32, v32 = s32.state()
+    p64, p32 = pressure(cfg, r64), pressure(cfg, r32)
+    assert np.linalg.norm(p32 - p64) <= 1e-5 * np.linalg.norm(p64)
+    assert np.linalg.norm(v32 - v64) <= 1e-5 * np.linalg.norm(v64)
