@@ -113,6 +113,35 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
             S.fl[F.a][F.side][F.fi] = (F.side ? -0.5f : 0.5f) * (ro[r] + S.r[F.nf]);
         }
         __syncthreads();
+        if constexpr (K >= 5) {
+            constexpr int WPA = (K2 + 31) / 32;
+            const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
+            if (live && a < 3 && t < K2) {
+                const int st = axis_stride<K>(a);
+                const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
+                float v[K];
+#pragma unroll
+                for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+                const float f0 = S.fl[a][0][t], fN = S.fl[a][1][t];
+                const float gs = P.gscale[a];
+#pragma unroll
+                for (int i = 0; i < K; i++) {
+                    float d[K], l0, ln;
+                    batch_row<K>(P, i, d, l0, ln);
+                    float s2 = l0 * f0;
+                    s2 += ln * fN;
+#pragma unroll
+                    for (int j = 0; j < K; j++) s2 += d[j] * v[j];
+                    S.out[a][b0 + i * st] = gs * s2;
+                }
+            }
+            __syncthreads();
+            if (act)
+#pragma unroll
+                for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = S.out[a2][n];
+            __syncthreads();
+            continue;
+        }
         if (act) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
@@ -223,10 +252,47 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
                                                      (F.side ? -0.5f : 0.5f) * (qo[r] + S.q[F.a][F.nf]));
         }
         __syncthreads();
+        if constexpr (K >= 5) {
+            // Line owners (see incr_stage_kernel): one warp (two for K = 6)
+            // per axis, a lane per line; the per-axis results, already times
+            // 1/w_a, reuse S.m (density) and S.q (momentum).
+            constexpr int WPA = (K2 + 31) / 32;
+            const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
+            if (live && a < 3 && t < K2) {
+                const int st = axis_stride<K>(a);
+                const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
+                float2 v[K];
+#pragma unroll
+                for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st];
+                const float2 g0 = S.g[a][0][t], gN = S.g[a][1][t];
+                const float iw = P.invw[a];
+#pragma unroll
+                for (int i = 0; i < K; i++) {
+                    float d[K], l0, ln;
+                    batch_row<K>(P, i, d, l0, ln);
+                    float sm = l0 * g0.x, sr = l0 * g0.y;
+                    sm += ln * gN.x;
+                    sr += ln * gN.y;
+#pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        sm += d[j] * v[j].x;
+                        sr += d[j] * v[j].y;
+                    }
+                    S.m[a][b0 + i * st] = iw * sr;
+                    S.q[a][b0 + i * st] = iw * sm;
+                }
+            }
+            __syncthreads();
+        }
         if (act) {
             float r_rho = 0.f, r_u[3];
 #pragma unroll
             for (int a = 0; a < 3; a++) {
+                if constexpr (K >= 5) {
+                    r_rho += S.m[a][n];
+                    r_u[a] = S.q[a][n];
+                    continue;
+                }
                 const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
                 const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
                 float d[K], l0, ln;
