@@ -187,7 +187,7 @@ __device__ __forceinline__ void exterior(const MeshDev<T>& m, const OpConst<T, K
 }
 
 template <int K>
-__device__ __forceinline__ int axis_stride(int a)
+__host__ __device__ constexpr int axis_stride(int a)
 {
     return a == 0 ? K * K : (a == 1 ? K : 1);
 }
@@ -240,6 +240,64 @@ struct OpRows {
         }
     }
 };
+
+// First node of line t along axis A (lines numbered like the face nodes fi),
+// for the line owners below.
+template <int A, int K>
+__device__ __forceinline__ int line_base(int t)
+{
+    return A == 0 ? t : (A == 1 ? (t % K) * K * K + t / K : t * K);
+}
+
+// One line of the LDG gradient along axis A.  A is a compile-time constant
+// so that the operator rows (kernel parameters) are constant-bank operands of
+// the FMAs rather than indexed constant loads.
+template <int A, typename T, int K, typename Smem>
+__device__ __forceinline__ void grad_line(const OpConst<T, K>& Cv, Smem& S, int t)
+{
+    constexpr int st = axis_stride<K>(A);
+    const int b0 = line_base<A, K>(t);
+    T v[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+    const T f0 = S.fl[A][0][t], fN = S.fl[A][1][t];
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        const T* row = Cv.rows[A][i];
+        T s2 = row[K] * f0;
+        s2 += row[K + 1] * fN;
+#pragma unroll
+        for (int j = 0; j < K; j++) s2 += row[j] * v[j];
+        S.out[A][b0 + i * st] = s2;
+    }
+}
+
+// One line of the stage operator along axis A: momentum and density sums of
+// the line's K outputs into S.q and S.m.
+template <int A, typename T, int K, typename Smem>
+__device__ __forceinline__ void stage_line(const OpConst<T, K>& Cv, Smem& S, int t)
+{
+    constexpr int st = axis_stride<K>(A);
+    const int b0 = line_base<A, K>(t);
+    typename Pair<T>::type v[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = S.f[A][b0 + j * st];
+    const typename Pair<T>::type g0 = S.g[A][0][t], gN = S.g[A][1][t];
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        const T* row = Cv.rows[A][i];
+        T sm = row[K] * g0.x, sr = row[K] * g0.y;
+        sm += row[K + 1] * gN.x;
+        sr += row[K + 1] * gN.y;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            sm += row[j] * v[j].x;
+            sr += row[j] * v[j].y;
+        }
+        S.m[A][b0 + i * st] = sr;
+        S.q[A][b0 + i * st] = sm;
+    }
+}
 
 // Resident CTAs per SM asked of the compiler for the gradient kernel (0: no
 // request): the FP32 kernel waits on memory latency and fits in 40 registers
@@ -310,21 +368,9 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         constexpr int WPA = (K2 + 31) / 32;
         const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
         if (live && a < 3 && t < K2) {
-            const int st = axis_stride<K>(a);
-            const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
-            T v[K];
-#pragma unroll
-            for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
-            const T f0 = S.fl[a][0][t], fN = S.fl[a][1][t];
-#pragma unroll
-            for (int i = 0; i < K; i++) {
-                const T* row = Cv.rows[a][i];
-                T s2 = row[K] * f0;
-                s2 += row[K + 1] * fN;
-#pragma unroll
-                for (int j = 0; j < K; j++) s2 += row[j] * v[j];
-                S.out[a][b0 + i * st] = s2;
-            }
+            if (a == 0) grad_line<0>(Cv, S, t);
+            else if (a == 1) grad_line<1>(Cv, S, t);
+            else grad_line<2>(Cv, S, t);
         }
         __syncthreads();
         if (!act) return;
@@ -607,26 +653,9 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
         constexpr int WPA = (K2 + 31) / 32;
         const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
         if (live && a < 3 && t < K2) {
-            const int st = axis_stride<K>(a);
-            const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
-            typename Pair<T>::type v[K];
-#pragma unroll
-            for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st];
-            const typename Pair<T>::type g0 = S.g[a][0][t], gN = S.g[a][1][t];
-#pragma unroll
-            for (int i = 0; i < K; i++) {
-                const T* row = Cv.rows[a][i];
-                T sm = row[K] * g0.x, sr = row[K] * g0.y;
-                sm += row[K + 1] * gN.x;
-                sr += row[K + 1] * gN.y;
-#pragma unroll
-                for (int j = 0; j < K; j++) {
-                    sm += row[j] * v[j].x;
-                    sr += row[j] * v[j].y;
-                }
-                S.m[a][b0 + i * st] = sr;
-                S.q[a][b0 + i * st] = sm;
-            }
+            if (a == 0) stage_line<0>(Cv, S, t);
+            else if (a == 1) stage_line<1>(Cv, S, t);
+            else stage_line<2>(Cv, S, t);
         }
         __syncthreads();
         if (!act) return;
