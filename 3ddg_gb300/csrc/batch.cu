@@ -22,6 +22,10 @@
 
 namespace dg {
 
+// Tile counters: [stage][order][phase].
+constexpr int kCounters = 3 * (BATCH_KMAX + 1) * 2;
+
+
 #define DGB_CUDA(call)                                                                         \
     do {                                                                                       \
         cudaError_t _e = (call);                                                               \
@@ -82,13 +86,20 @@ int Batch::init(int device_capacity)
     cudaDeviceProp prop;
     DGB_CUDA(cudaGetDeviceProperties(&prop, device));
     num_sms = prop.multiProcessorCount;
-    int occ = 0;
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel, BATCH_THREADS, 0));
-    max_ctas_per_sm = std::max(1, occ);
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2], batch_stage_kernel<2>, BATCH_THREADS, 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3], batch_stage_kernel<3>, BATCH_THREADS, 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4], batch_stage_kernel<4>, BATCH_THREADS, 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5], batch_stage_kernel<5>, BATCH_THREADS, 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6], batch_stage_kernel<6>, BATCH_THREADS, 0));
+    max_ctas_per_sm = 1;
+    for (int k = 2; k <= BATCH_KMAX; k++) {
+        occ_k[k] = std::max(1, occ_k[k]);
+        max_ctas_per_sm = std::max(max_ctas_per_sm, occ_k[k]);
+    }
     ctas_per_sm = max_ctas_per_sm;
     capacity = std::max(1, device_capacity);
     DGB_CUDA(cudaMalloc(&d_probs, capacity * sizeof(BatchProblem)));
-    DGB_CUDA(cudaMalloc(&d_counters, 6 * sizeof(int)));
+    DGB_CUDA(cudaMalloc(&d_counters, kCounters * sizeof(int)));
     for (int k = 0; k <= BATCH_KMAX; k++) passes[k] = 4;
     return DG_OK;
 }
@@ -237,6 +248,7 @@ int Batch::remove(int i)
 void Batch::build_tiles()
 {
     tiles.clear();
+    for (int k = 0; k <= BATCH_KMAX; k++) tile_begin[k] = tile_end[k] = 0;
     // largest orders first: the atomic tile counter then hands out the
     // longest tiles early and the short ones fill the tail
     std::vector<int> order(probs.size());
@@ -246,6 +258,7 @@ void Batch::build_tiles()
         const Entry& E = probs[i];
         const int K = E.K;
         const int chunk = bepb_of(K) * std::max(1, passes[K]);
+        if (tile_begin[K] == tile_end[K]) tile_begin[K] = tile_end[K] = (int)tiles.size();
         for (int e0 = 0; e0 < E.n_elem; e0 += chunk) {
             BatchTile t;
             t.prob = i;
@@ -254,6 +267,7 @@ void Batch::build_tiles()
             t.K = K;
             tiles.push_back(t);
         }
+        tile_end[K] = (int)tiles.size();
     }
 }
 
@@ -280,29 +294,42 @@ int Batch::upload_tiles()
 int Batch::launch_step()
 {
     const int n = (int)probs.size();
-    DGB_CUDA(cudaMemsetAsync(d_counters, 0, 6 * sizeof(int), stream));
+    DGB_CUDA(cudaMemsetAsync(d_counters, 0, kCounters * sizeof(int), stream));
     batch_step_begin<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
+    launches += 2;
     for (int s = 0; s < 3; s++) {
-        BatchArgs A;
-        A.probs = d_probs;
-        A.tiles = d_tiles;
-        A.n_tiles = (int)tiles.size();
-        A.counters = d_counters + 2 * s;
-        A.stage = s;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(num_sms * ctas_per_sm);
-        cfg.blockDim = dim3(BATCH_THREADS);
-        cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        DGB_CUDA(cudaLaunchKernelEx(&cfg, batch_stage_kernel, A));
+        for (int K = BATCH_KMAX; K >= 2; K--) {
+            if (tile_end[K] == tile_begin[K]) continue;
+            BatchArgs A;
+            A.probs = d_probs;
+            A.tiles = d_tiles;
+            A.tile0 = tile_begin[K];
+            A.n_tiles = tile_end[K] - tile_begin[K];
+            A.counters = d_counters + 2 * (s * (BATCH_KMAX + 1) + K);
+            A.stage = s;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(num_sms * std::min(ctas_per_sm, occ_k[K]));
+            cfg.blockDim = dim3(BATCH_THREADS);
+            cfg.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            cudaError_t e = cudaSuccess;
+            switch (K) {
+            case 2: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<2>, A); break;
+            case 3: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<3>, A); break;
+            case 4: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<4>, A); break;
+            case 5: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<5>, A); break;
+            case 6: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<6>, A); break;
+            }
+            DGB_CUDA(e);
+            launches++;
+        }
     }
     batch_step_end<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
     DGB_CUDA(cudaGetLastError());
-    launches += 5;
     return DG_OK;
 }
 
@@ -316,7 +343,10 @@ int Batch::step(int nsteps)
     if (use_graph && !graph) {
         cudaGraph_t g = nullptr;
         DGB_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = launches;
         int rc = launch_step();
+        step_kernels = launches - before;  // kernels per replay; nothing ran during capture
+        launches = before;
         cudaError_t ec = cudaStreamEndCapture(stream, &g);
         if (rc || ec != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -335,7 +365,7 @@ int Batch::step(int nsteps)
     for (int i = 0; i < nsteps; i++) {
         if (graph) {
             DGB_CUDA(cudaGraphLaunch(graph, stream));
-            launches += 5;
+            launches += step_kernels;
         } else {
             int rc = launch_step();
             if (rc) return rc;

@@ -37,6 +37,9 @@ struct Batch {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 0, max_ctas_per_sm = 1, ctas_per_sm = 1;
+    int occ_k[BATCH_KMAX + 1] = {};          // resident CTAs per SM of each order's kernel
+    int tile_begin[BATCH_KMAX + 1] = {}, tile_end[BATCH_KMAX + 1] = {};  // each order's tile range
+    long long step_kernels = 0;  // kernels in one captured step
     int passes[BATCH_KMAX + 1];  // autotuned: passes of EPB(K) elements per tile
     std::vector<Entry> probs;
     std::vector<BatchProblem> saved_desc;

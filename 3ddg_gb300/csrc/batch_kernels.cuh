@@ -333,19 +333,19 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
     }
 }
 
-// Shared memory of one CTA: the largest per-order need.
+// Shared memory of one CTA of order K.
+template <int K>
 __host__ __device__ constexpr size_t batch_smem_bytes()
 {
-    size_t m = 0;
-    const size_t s2 = bepb_of(2) * sizeof(PlainSmem<float, 2>), s3 = bepb_of(3) * sizeof(PlainSmem<float, 3>);
-    const size_t s4 = bepb_of(4) * sizeof(PlainSmem<float, 4>), s5 = bepb_of(5) * sizeof(PlainSmem<float, 5>);
-    const size_t s6 = bepb_of(6) * sizeof(PlainSmem<float, 6>);
-    m = s2 > m ? s2 : m;
-    m = s3 > m ? s3 : m;
-    m = s4 > m ? s4 : m;
-    m = s5 > m ? s5 : m;
-    m = s6 > m ? s6 : m;
-    return m;
+    return bepb_of(K) * sizeof(PlainSmem<float, K>);
+}
+
+// Resident CTAs per SM asked of the compiler for order K (register budget
+// 65536 / (256 x blocks)): the most that each order's path fits without
+// spilling (K = 3 spills 36 bytes at 4, K = 2 fits 48 registers, K = 4 40).
+__host__ __device__ constexpr int batch_min_blocks(int K)
+{
+    return K == 2 ? 5 : (K == 4 ? 6 : 4);
 }
 
 __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProblem* src)
@@ -355,11 +355,14 @@ __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProbl
     for (int i = threadIdx.x; i < (int)(sizeof(BatchProblem) / sizeof(int)); i += blockDim.x) d[i] = s[i];
 }
 
-// One RK stage of every active problem: LDG gradient of every tile, grid
-// barrier, stage update of every tile.
-__global__ void __launch_bounds__(BATCH_THREADS, 4) batch_stage_kernel(BatchArgs A)
+// One RK stage of every active problem of order K: LDG gradient of every
+// tile, grid barrier, stage update of every tile.  One kernel per order (its
+// tiles are a contiguous range of the tile list), so that each order gets its
+// own register budget and shared memory.
+template <int K>
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K)) batch_stage_kernel(BatchArgs A)
 {
-    __shared__ __align__(16) unsigned char smraw[batch_smem_bytes()];
+    __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
     __shared__ BatchProblem P;
     __shared__ int tile_idx;
     for (int phase = 0; phase < 2; phase++) {
@@ -369,27 +372,12 @@ __global__ void __launch_bounds__(BATCH_THREADS, 4) batch_stage_kernel(BatchArgs
             __syncthreads();
             const int ti = tile_idx;
             if (ti >= A.n_tiles) break;
-            const BatchTile T = A.tiles[ti];
+            const BatchTile T = A.tiles[A.tile0 + ti];
             load_problem(P, A.probs + T.prob);
             __syncthreads();
             if (P.active) {
-                if (phase == 0) {
-                    switch (T.K) {
-                    case 2: batch_grad_tile<2>(P, T, A.stage, smraw); break;
-                    case 3: batch_grad_tile<3>(P, T, A.stage, smraw); break;
-                    case 4: batch_grad_tile<4>(P, T, A.stage, smraw); break;
-                    case 5: batch_grad_tile<5>(P, T, A.stage, smraw); break;
-                    case 6: batch_grad_tile<6>(P, T, A.stage, smraw); break;
-                    }
-                } else {
-                    switch (T.K) {
-                    case 2: batch_stage_tile<2>(P, T, A.stage, smraw); break;
-                    case 3: batch_stage_tile<3>(P, T, A.stage, smraw); break;
-                    case 4: batch_stage_tile<4>(P, T, A.stage, smraw); break;
-                    case 5: batch_stage_tile<5>(P, T, A.stage, smraw); break;
-                    case 6: batch_stage_tile<6>(P, T, A.stage, smraw); break;
-                    }
-                }
+                if (phase == 0) batch_grad_tile<K>(P, T, A.stage, smraw);
+                else batch_stage_tile<K>(P, T, A.stage, smraw);
             }
             __syncthreads();
         }

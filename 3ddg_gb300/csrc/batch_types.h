@@ -42,7 +42,7 @@ struct BatchTile {
 struct BatchArgs {
     BatchProblem* probs;
     const BatchTile* tiles;
-    int n_tiles;
+    int tile0, n_tiles;    // this launch's tiles: tiles[tile0 .. tile0 + n_tiles)
     int* counters;         // [2]: phase-1 and phase-2 tile counters, zeroed before the launch
     int stage;
 };
