@@ -22,8 +22,6 @@
 
 namespace dg {
 
-// Tile counters: [stage][order][phase].
-constexpr int kCounters = 3 * (BATCH_KMAX + 1) * 2;
 
 
 #define DGB_CUDA(call)                                                                         \
@@ -99,7 +97,6 @@ int Batch::init(int device_capacity)
     ctas_per_sm = max_ctas_per_sm;
     capacity = std::max(1, device_capacity);
     DGB_CUDA(cudaMalloc(&d_probs, capacity * sizeof(BatchProblem)));
-    DGB_CUDA(cudaMalloc(&d_counters, kCounters * sizeof(int)));
     for (int k = 0; k <= BATCH_KMAX; k++) passes[k] = 4;
     return DG_OK;
 }
@@ -137,6 +134,7 @@ int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file
     if (!err.empty()) return fail(DG_ERR_INVALID, err);
 
     Entry E;
+    E.op_key = key;
     E.p = p;
     E.dt = dt;
     E.steps = steps;
@@ -248,17 +246,27 @@ int Batch::remove(int i)
 void Batch::build_tiles()
 {
     tiles.clear();
-    for (int k = 0; k <= BATCH_KMAX; k++) tile_begin[k] = tile_end[k] = 0;
-    // largest orders first: the atomic tile counter then hands out the
-    // longest tiles early and the short ones fill the tail
+    groups.clear();
+    // groups by order (largest first) and operator; within a group the
+    // atomic tile counter hands out the tiles in order
     std::vector<int> order(probs.size());
     for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return probs[a].K > probs[b].K; });
-    for (int i : order) {
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (probs[a].K != probs[b].K) return probs[a].K > probs[b].K;
+        return probs[a].op_key < probs[b].op_key;
+    });
+    for (size_t n = 0; n < order.size(); n++) {
+        const int i = order[n];
         const Entry& E = probs[i];
         const int K = E.K;
+        if (groups.empty() || groups.back().K != K || probs[order[n - 1]].op_key != E.op_key) {
+            Group g;
+            g.K = K;
+            g.begin = g.end = (int)tiles.size();
+            std::memcpy(g.ops.rows, E.desc.rows, sizeof g.ops.rows);
+            groups.push_back(g);
+        }
         const int chunk = bepb_of(K) * std::max(1, passes[K]);
-        if (tile_begin[K] == tile_end[K]) tile_begin[K] = tile_end[K] = (int)tiles.size();
         for (int e0 = 0; e0 < E.n_elem; e0 += chunk) {
             BatchTile t;
             t.prob = i;
@@ -267,13 +275,22 @@ void Batch::build_tiles()
             t.K = K;
             tiles.push_back(t);
         }
-        tile_end[K] = (int)tiles.size();
+        groups.back().end = (int)tiles.size();
     }
 }
 
 int Batch::upload_tiles()
 {
     build_tiles();
+    if ((int)groups.size() > counter_groups) {
+        // tile counters: [stage][group][phase]
+        DGB_CUDA(cudaStreamSynchronize(stream));
+        if (d_counters) cudaFree(d_counters);
+        d_counters = nullptr;
+        counter_groups = 0;
+        DGB_CUDA(cudaMalloc(&d_counters, 3 * groups.size() * 2 * sizeof(int)));
+        counter_groups = (int)groups.size();
+    }
     if ((int)tiles.size() > tile_capacity) {
         if (d_tiles) cudaFree(d_tiles);
         tile_capacity = std::max<int>((int)tiles.size(), 2 * tile_capacity);
@@ -294,18 +311,20 @@ int Batch::upload_tiles()
 int Batch::launch_step()
 {
     const int n = (int)probs.size();
-    DGB_CUDA(cudaMemsetAsync(d_counters, 0, kCounters * sizeof(int), stream));
+    const int G = (int)groups.size();
+    DGB_CUDA(cudaMemsetAsync(d_counters, 0, 3 * G * 2 * sizeof(int), stream));
     batch_step_begin<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
     launches += 2;
     for (int s = 0; s < 3; s++) {
-        for (int K = BATCH_KMAX; K >= 2; K--) {
-            if (tile_end[K] == tile_begin[K]) continue;
+        for (int g = 0; g < G; g++) {
+            const Group& grp = groups[g];
+            const int K = grp.K;
             BatchArgs A;
             A.probs = d_probs;
             A.tiles = d_tiles;
-            A.tile0 = tile_begin[K];
-            A.n_tiles = tile_end[K] - tile_begin[K];
-            A.counters = d_counters + 2 * (s * (BATCH_KMAX + 1) + K);
+            A.tile0 = grp.begin;
+            A.n_tiles = grp.end - grp.begin;
+            A.counters = d_counters + 2 * (s * G + g);
             A.stage = s;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(num_sms * std::min(ctas_per_sm, occ_k[K]));
@@ -318,11 +337,11 @@ int Batch::launch_step()
             cfg.numAttrs = 1;
             cudaError_t e = cudaSuccess;
             switch (K) {
-            case 2: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<2>, A); break;
-            case 3: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<3>, A); break;
-            case 4: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<4>, A); break;
-            case 5: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<5>, A); break;
-            case 6: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<6>, A); break;
+            case 2: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<2>, A, grp.ops); break;
+            case 3: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<3>, A, grp.ops); break;
+            case 4: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<4>, A, grp.ops); break;
+            case 5: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<5>, A, grp.ops); break;
+            case 6: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<6>, A, grp.ops); break;
             }
             DGB_CUDA(e);
             launches++;

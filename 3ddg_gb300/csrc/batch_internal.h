@@ -31,6 +31,7 @@ struct Batch {
         int* nbr = nullptr;
         float* sigma = nullptr;
         BatchProblem desc;     // host copy of the device descriptor
+        std::string op_key;    // order | mass matrix | basis files
         long long id = 0;
     };
 
@@ -38,7 +39,14 @@ struct Batch {
     cudaStream_t stream = nullptr;
     int num_sms = 0, max_ctas_per_sm = 1, ctas_per_sm = 1;
     int occ_k[BATCH_KMAX + 1] = {};          // resident CTAs per SM of each order's kernel
-    int tile_begin[BATCH_KMAX + 1] = {}, tile_end[BATCH_KMAX + 1] = {};  // each order's tile range
+    // Problems of one order sharing one operator (order, mass matrix, basis
+    // files) form a group: one kernel launch per group and stage.
+    struct Group {
+        int K = 0, begin = 0, end = 0;  // tiles[begin .. end)
+        BatchOps ops{};
+    };
+    std::vector<Group> groups;
+    int counter_groups = 0;  // groups d_counters has room for
     long long step_kernels = 0;  // kernels in one captured step
     int passes[BATCH_KMAX + 1];  // autotuned: passes of EPB(K) elements per tile
     std::vector<Entry> probs;

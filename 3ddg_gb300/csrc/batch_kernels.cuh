@@ -61,7 +61,8 @@ __device__ __forceinline__ void batch_row(const BatchProblem& P, int ia, float d
 }
 
 template <int K>
-__device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
+__device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, const BatchTile& T, int stage,
+                                unsigned char* smraw)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K2;
     constexpr int R = (NF + NPT - 1) / NPT;
@@ -126,12 +127,11 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
                 const float gs = P.gscale[a];
 #pragma unroll
                 for (int i = 0; i < K; i++) {
-                    float d[K], l0, ln;
-                    batch_row<K>(P, i, d, l0, ln);
-                    float s2 = l0 * f0;
-                    s2 += ln * fN;
+                    const float* row = ops.rows[i];  // constant-bank operands
+                    float s2 = row[K] * f0;
+                    s2 += row[K + 1] * fN;
 #pragma unroll
-                    for (int j = 0; j < K; j++) s2 += d[j] * v[j];
+                    for (int j = 0; j < K; j++) s2 += row[j] * v[j];
                     S.out[a][b0 + i * st] = gs * s2;
                 }
             }
@@ -161,7 +161,8 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchTile& T, int s
 }
 
 template <int K>
-__device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int stage, unsigned char* smraw)
+__device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, const BatchTile& T, int stage,
+                                 unsigned char* smraw)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K2;
     constexpr int R = (NF + NPT - 1) / NPT;
@@ -268,15 +269,14 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchTile& T, int 
                 const float iw = P.invw[a];
 #pragma unroll
                 for (int i = 0; i < K; i++) {
-                    float d[K], l0, ln;
-                    batch_row<K>(P, i, d, l0, ln);
-                    float sm = l0 * g0.x, sr = l0 * g0.y;
-                    sm += ln * gN.x;
-                    sr += ln * gN.y;
+                    const float* row = ops.rows[i];  // constant-bank operands
+                    float sm = row[K] * g0.x, sr = row[K] * g0.y;
+                    sm += row[K + 1] * gN.x;
+                    sr += row[K + 1] * gN.y;
 #pragma unroll
                     for (int j = 0; j < K; j++) {
-                        sm += d[j] * v[j].x;
-                        sr += d[j] * v[j].y;
+                        sm += row[j] * v[j].x;
+                        sr += row[j] * v[j].y;
                     }
                     S.m[a][b0 + i * st] = iw * sr;
                     S.q[a][b0 + i * st] = iw * sm;
@@ -360,7 +360,7 @@ __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProbl
 // tiles are a contiguous range of the tile list), so that each order gets its
 // own register budget and shared memory.
 template <int K>
-__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K)) batch_stage_kernel(BatchArgs A)
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K)) batch_stage_kernel(BatchArgs A, const BatchOps ops)
 {
     __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
     __shared__ BatchProblem P;
@@ -376,8 +376,8 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K)) batch_stag
             load_problem(P, A.probs + T.prob);
             __syncthreads();
             if (P.active) {
-                if (phase == 0) batch_grad_tile<K>(P, T, A.stage, smraw);
-                else batch_stage_tile<K>(P, T, A.stage, smraw);
+                if (phase == 0) batch_grad_tile<K>(P, ops, T, A.stage, smraw);
+                else batch_stage_tile<K>(P, ops, T, A.stage, smraw);
             }
             __syncthreads();
         }

@@ -35,6 +35,13 @@ struct BatchProblem {
     long long steps_done;
 };
 
+// The unit-interval operator rows of one order (same layout as
+// BatchProblem::rows), passed by value to the kernel of a group of problems
+// that share them, so that the line owners read constant-bank operands.
+struct BatchOps {
+    float rows[BATCH_KMAX][8];
+};
+
 struct BatchTile {
     int prob, e0, count, K;
 };
