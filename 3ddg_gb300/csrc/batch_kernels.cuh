@@ -1,19 +1,21 @@
 // Batched form: many independent problems of uneven element counts and
 // orders advanced together, FP32 fields/fluxes/stages with the
-// Kahan-compensated update, one persistent kernel per RK stage.
+// Kahan-compensated update.
 //
 // Each problem keeps its own device buffers and a device descriptor
 // (BatchProblem) with its FP32 operators, RK weights, time and source state,
 // so problems can join and leave (the serving form) without touching the
-// others.  A stage launch is a cooperative persistent grid that pulls tiles
-// (problem, first element, element count) from a work list with an atomic
-// counter: phase 1 computes the LDG gradient of every tile, a grid-wide
-// barrier, phase 2 the stage update of every tile.  A tile runs the code path
-// of its problem's order (K = N + 1 <= 6) with EPB(K) elements per pass of a
-// 256-thread CTA; the number of passes per tile (tile size) is chosen per
-// order by the autotuner.  The arithmetic per element is the one of
-// stage_kernel / ldg_gradient_kernel (dg_kernels.cuh) with 1/w_a applied after
-// the line sums, so one descriptor serves all three stages.
+// others.  Problems of one order that share one operator form a group; per
+// RK stage each group gets one cooperative persistent kernel of its order
+// (batch_stage_kernel<K>, K = N + 1 <= 6) that pulls tiles (problem, first
+// element, element count) from an atomic counter: phase 1 computes the LDG
+// gradient of every tile, a grid-wide barrier, phase 2 the stage update of
+// every tile, with EPB(K) elements per pass of a 256-thread CTA; the number
+// of passes per tile (tile size) is chosen per order by the autotuner.  The
+// arithmetic per element is the one of incr_stage_kernel /
+// ldg_gradient_kernel (dg_kernels.cuh) with 1/w_a applied after the line
+// sums, so one descriptor serves all three stages and the group's operator
+// rows (kernel parameters) do not depend on the axis.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -43,21 +45,6 @@ __device__ __forceinline__ float batch_in(const BatchProblem& P, const float* ub
     float v = __ldg(ub + (size_t)f * P.fs + off);
     if (inc) v += __ldg(inc + (size_t)f * P.fs + off);
     return v;
-}
-
-// Row ia of the problem's operator (D row, then the two lift entries) from
-// the shared-memory descriptor into registers: two 16-byte loads.
-template <int K>
-__device__ __forceinline__ void batch_row(const BatchProblem& P, int ia, float d[K], float& l0, float& ln)
-{
-    float row[8];
-    const float4* src = reinterpret_cast<const float4*>(P.rows[ia]);
-    reinterpret_cast<float4*>(row)[0] = src[0];
-    reinterpret_cast<float4*>(row)[1] = src[1];
-#pragma unroll
-    for (int j = 0; j < K; j++) d[j] = row[j];
-    l0 = row[K];
-    ln = row[K + 1];
 }
 
 template <int K>
@@ -114,10 +101,21 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
             S.fl[F.a][F.side][F.fi] = (F.side ? -0.5f : 0.5f) * (ro[r] + S.r[F.nf]);
         }
         __syncthreads();
-        if constexpr (K >= 5) {
+        {
             constexpr int WPA = (K2 + 31) / 32;
-            const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
-            if (live && a < 3 && t < K2) {
+            int a, t, ls;
+            if constexpr (K >= 5) {
+                const int w = n / 32;
+                a = w / WPA;
+                t = (w % WPA) * 32 + n % 32;
+                ls = slot;
+            } else {
+                ls = threadIdx.x / (3 * K2);
+                a = (threadIdx.x / K2) % 3;
+                t = threadIdx.x % K2;
+            }
+            GradSmem<float, K>& S = SM[ls < EPB ? ls : 0];
+            if (ls < EPB && c0 + ls < T.e0 + T.count && a < 3 && t < K2) {
                 const int st = axis_stride<K>(a);
                 const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
                 float v[K];
@@ -136,26 +134,10 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
                 }
             }
             __syncthreads();
-            if (act)
-#pragma unroll
-                for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = S.out[a2][n];
-            __syncthreads();
-            continue;
         }
-        if (act) {
+        if (act)
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
-                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                float d[K], l0, ln;
-                batch_row<K>(P, ia, d, l0, ln);
-                float s = l0 * S.fl[a][0][fi];
-                s += ln * S.fl[a][1][fi];
-#pragma unroll
-                for (int j = 0; j < K; j++) s += d[j] * S.r[base + j * st];
-                P.q[(size_t)a * P.fs + (size_t)e * P.np + n] = P.gscale[a] * s;
-            }
-        }
+            for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = S.out[a2][n];
         __syncthreads();
     }
 }
@@ -253,13 +235,25 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
                                                      (F.side ? -0.5f : 0.5f) * (qo[r] + S.q[F.a][F.nf]));
         }
         __syncthreads();
-        if constexpr (K >= 5) {
-            // Line owners (see incr_stage_kernel): one warp (two for K = 6)
-            // per axis, a lane per line; the per-axis results, already times
-            // 1/w_a, reuse S.m (density) and S.q (momentum).
+        {
+            // Line owners (see incr_stage_kernel); the per-axis results, already
+            // times 1/w_a, reuse S.m (density) and S.q (momentum).  K >= 5: one
+            // warp (two for K = 6) per axis of each element slot, a lane per
+            // line; K <= 4: the CTA's threads over (slot, axis, line).
             constexpr int WPA = (K2 + 31) / 32;
-            const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
-            if (live && a < 3 && t < K2) {
+            int a, t, ls;
+            if constexpr (K >= 5) {
+                const int w = n / 32;
+                a = w / WPA;
+                t = (w % WPA) * 32 + n % 32;
+                ls = slot;
+            } else {
+                ls = threadIdx.x / (3 * K2);
+                a = (threadIdx.x / K2) % 3;
+                t = threadIdx.x % K2;
+            }
+            PlainSmem<float, K>& S = SM[ls < EPB ? ls : 0];
+            if (ls < EPB && c0 + ls < T.e0 + T.count && a < 3 && t < K2) {
                 const int st = axis_stride<K>(a);
                 const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
                 float2 v[K];
@@ -288,28 +282,8 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
             float r_rho = 0.f, r_u[3];
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                if constexpr (K >= 5) {
-                    r_rho += S.m[a][n];
-                    r_u[a] = S.q[a][n];
-                    continue;
-                }
-                const int st = axis_stride<K>(a), ia = c[a], base = n - ia * st;
-                const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-                float d[K], l0, ln;
-                batch_row<K>(P, ia, d, l0, ln);
-                const float2 g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-                float sm = l0 * g0.x, sr = l0 * g0.y;
-                sm += ln * gN.x;
-                sr += ln * gN.y;
-#pragma unroll
-                for (int j = 0; j < K; j++) {
-                    const float dj = d[j];
-                    const float2 v = S.f[a][base + j * st];
-                    sm += dj * v.x;
-                    sr += dj * v.y;
-                }
-                r_rho += P.invw[a] * sr;
-                r_u[a] = P.invw[a] * sm;
+                r_rho += S.m[a][n];
+                r_u[a] = S.q[a][n];
             }
             const float ks = ca * sig;
             const float cbe = cb - ks, ce = eps - ks;
@@ -342,7 +316,7 @@ __host__ __device__ constexpr size_t batch_smem_bytes()
 
 // Resident CTAs per SM asked of the compiler for order K (register budget
 // 65536 / (256 x blocks)): the most that each order's path fits without
-// spilling (K = 3 spills 36 bytes at 4, K = 2 fits 48 registers, K = 4 40).
+// spilling (K = 2 in 48 registers, K = 4 in 40, the others in 64).
 __host__ __device__ constexpr int batch_min_blocks(int K)
 {
     return K == 2 ? 5 : (K == 4 ? 6 : 4);
