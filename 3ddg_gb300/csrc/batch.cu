@@ -81,6 +81,11 @@ int Batch::init(int device_capacity)
 {
     DGB_CUDA(cudaGetDevice(&device));
     DGB_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (int i = 0; i < kBranches; i++) {
+        DGB_CUDA(cudaStreamCreateWithFlags(&branch[i], cudaStreamNonBlocking));
+        DGB_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+    }
+    DGB_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
     cudaDeviceProp prop;
     DGB_CUDA(cudaGetDeviceProperties(&prop, device));
     num_sms = prop.multiProcessorCount;
@@ -315,10 +320,15 @@ int Batch::launch_step()
     DGB_CUDA(cudaMemsetAsync(d_counters, 0, 3 * G * 2 * sizeof(int), stream));
     batch_step_begin<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
     launches += 2;
-    for (int s = 0; s < 3; s++) {
-        for (int g = 0; g < G; g++) {
-            const Group& grp = groups[g];
-            const int K = grp.K;
+    // fork: group g runs its three stages on branch g % kBranches
+    const int nb = std::min(G, (int)kBranches);
+    DGB_CUDA(cudaEventRecord(fork_ev, stream));
+    for (int b = 0; b < nb; b++) DGB_CUDA(cudaStreamWaitEvent(branch[b], fork_ev, 0));
+    for (int g = 0; g < G; g++) {
+        const Group& grp = groups[g];
+        const int K = grp.K;
+        cudaStream_t bs = branch[g % kBranches];
+        for (int s = 0; s < 3; s++) {
             BatchArgs A;
             A.probs = d_probs;
             A.tiles = d_tiles;
@@ -326,26 +336,26 @@ int Batch::launch_step()
             A.n_tiles = grp.end - grp.begin;
             A.counters = d_counters + 2 * (s * G + g);
             A.stage = s;
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(num_sms * std::min(ctas_per_sm, occ_k[K]));
-            cfg.blockDim = dim3(BATCH_THREADS);
-            cfg.stream = stream;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeCooperative;
-            attr[0].val.cooperative = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            cudaError_t e = cudaSuccess;
-            switch (K) {
-            case 2: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<2>, A, grp.ops); break;
-            case 3: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<3>, A, grp.ops); break;
-            case 4: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<4>, A, grp.ops); break;
-            case 5: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<5>, A, grp.ops); break;
-            case 6: e = cudaLaunchKernelEx(&cfg, batch_stage_kernel<6>, A, grp.ops); break;
+            // persistent grid, but no more CTAs than the group has tiles: a small
+            // group (few problems in flight) leaves room for the other branches
+            const int grid = std::max(1, std::min(num_sms * std::min(ctas_per_sm, occ_k[K]), A.n_tiles));
+            for (int phase = 0; phase < 2; phase++) {
+                switch (K) {
+                case 2: batch_stage_kernel<2><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                case 3: batch_stage_kernel<3><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                case 4: batch_stage_kernel<4><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                case 5: batch_stage_kernel<5><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                case 6: batch_stage_kernel<6><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                }
+                DGB_CUDA(cudaGetLastError());
+                launches++;
             }
-            DGB_CUDA(e);
-            launches++;
         }
+    }
+    // join
+    for (int b = 0; b < nb; b++) {
+        DGB_CUDA(cudaEventRecord(join_ev[b], branch[b]));
+        DGB_CUDA(cudaStreamWaitEvent(stream, join_ev[b], 0));
     }
     batch_step_end<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
     DGB_CUDA(cudaGetLastError());
@@ -550,6 +560,14 @@ size_t Batch::total_nodes() const
 Batch::~Batch()
 {
     if (stream) cudaStreamSynchronize(stream);
+    for (int i = 0; i < kBranches; i++) {
+        if (branch[i]) {
+            cudaStreamSynchronize(branch[i]);
+            cudaStreamDestroy(branch[i]);
+        }
+        if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
     if (graph) cudaGraphExecDestroy(graph);
     for (Entry& E : probs) {
         cudaFree(E.data);

@@ -37,6 +37,12 @@ struct Batch {
 
     int device = 0;
     cudaStream_t stream = nullptr;
+    // Branch streams: the groups' stage kernels run as parallel branches of
+    // the step (each group's three stages in order on its branch), joined
+    // before the step's end.
+    static constexpr int kBranches = 6;
+    cudaStream_t branch[kBranches] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[kBranches] = {};
     int num_sms = 0, max_ctas_per_sm = 1, ctas_per_sm = 1;
     int occ_k[BATCH_KMAX + 1] = {};          // resident CTAs per SM of each order's kernel
     // Problems of one order sharing one operator (order, mass matrix, basis

@@ -6,19 +6,18 @@
 // (BatchProblem) with its FP32 operators, RK weights, time and source state,
 // so problems can join and leave (the serving form) without touching the
 // others.  Problems of one order that share one operator form a group; per
-// RK stage each group gets one cooperative persistent kernel of its order
-// (batch_stage_kernel<K>, K = N + 1 <= 6) that pulls tiles (problem, first
-// element, element count) from an atomic counter: phase 1 computes the LDG
-// gradient of every tile, a grid-wide barrier, phase 2 the stage update of
-// every tile, with EPB(K) elements per pass of a 256-thread CTA; the number
-// of passes per tile (tile size) is chosen per order by the autotuner.  The
+// RK stage each group gets two launches of a persistent kernel of its order
+// (batch_stage_kernel<K>, K = N + 1 <= 6) that pull tiles (problem, first
+// element, element count) from an atomic counter: the LDG gradient of every
+// tile, then the stage update of every tile, with EPB(K) elements per pass of
+// a 256-thread CTA; the number of passes per tile (tile size) is chosen per
+// order by the autotuner.  Groups run as parallel branches of the step.  The
 // arithmetic per element is the one of incr_stage_kernel /
 // ldg_gradient_kernel (dg_kernels.cuh) with 1/w_a applied after the line
 // sums, so one descriptor serves all three stages and the group's operator
 // rows (kernel parameters) do not depend on the axis.
 #pragma once
 
-#include <cooperative_groups.h>
 
 #include "batch_types.h"
 #include "dg_kernels.cuh"
@@ -329,32 +328,32 @@ __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProbl
     for (int i = threadIdx.x; i < (int)(sizeof(BatchProblem) / sizeof(int)); i += blockDim.x) d[i] = s[i];
 }
 
-// One RK stage of every active problem of order K: LDG gradient of every
-// tile, grid barrier, stage update of every tile.  One kernel per order (its
-// tiles are a contiguous range of the tile list), so that each order gets its
-// own register budget and shared memory.
+// One phase of one RK stage of every active problem of a group of order K:
+// phase 0 the LDG gradient of every tile, phase 1 the stage update of every
+// tile.  The two phases are separate launches (the kernel boundary is the
+// barrier between them), so that groups can run as parallel branches of the
+// step without any kernel waiting on another's blocks.  A persistent grid
+// pulls the group's tiles from an atomic counter.
 template <int K>
-__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K)) batch_stage_kernel(BatchArgs A, const BatchOps ops)
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K))
+    batch_stage_kernel(BatchArgs A, const BatchOps ops, int phase)
 {
     __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
     __shared__ BatchProblem P;
     __shared__ int tile_idx;
-    for (int phase = 0; phase < 2; phase++) {
-        if (phase == 1) cooperative_groups::this_grid().sync();
-        for (;;) {
-            if (threadIdx.x == 0) tile_idx = atomicAdd(A.counters + phase, 1);
-            __syncthreads();
-            const int ti = tile_idx;
-            if (ti >= A.n_tiles) break;
-            const BatchTile T = A.tiles[A.tile0 + ti];
-            load_problem(P, A.probs + T.prob);
-            __syncthreads();
-            if (P.active) {
-                if (phase == 0) batch_grad_tile<K>(P, ops, T, A.stage, smraw);
-                else batch_stage_tile<K>(P, ops, T, A.stage, smraw);
-            }
-            __syncthreads();
+    for (;;) {
+        if (threadIdx.x == 0) tile_idx = atomicAdd(A.counters + phase, 1);
+        __syncthreads();
+        const int ti = tile_idx;
+        if (ti >= A.n_tiles) break;
+        const BatchTile T = A.tiles[A.tile0 + ti];
+        load_problem(P, A.probs + T.prob);
+        __syncthreads();
+        if (P.active) {
+            if (phase == 0) batch_grad_tile<K>(P, ops, T, A.stage, smraw);
+            else batch_stage_tile<K>(P, ops, T, A.stage, smraw);
         }
+        __syncthreads();
     }
 }
 

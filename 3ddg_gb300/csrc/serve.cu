@@ -45,6 +45,8 @@ struct Server {
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     long long ticks = 0;
     double inflight_sum = 0.0;
+    double step_s = 0.0;  // running estimate of the wall time of one batch step
+    static constexpr int kMaxStepsPerTick = 64;
 
     double now() const
     {
@@ -118,19 +120,40 @@ struct Server {
         return DG_OK;
     }
 
-    // One iteration: admit, advance every in-flight solve one step, retire.
+    // Steps the next tick may run without delaying a retirement or the
+    // admission of the next arrival: up to the first in-flight solve's end,
+    // and only as many steps as fit before the next pending arrival.
+    int steps_this_tick(double t) const
+    {
+        int k = kMaxStepsPerTick;
+        for (long long id : inflight) k = std::min(k, reqs.at(id).remaining);
+        if (!pending.empty()) {
+            const double wait = reqs.at(pending.front()).t_arrival - t;
+            if (wait <= 0.0) return 1;  // arrived, waiting for memory: retire as soon as possible
+            if (step_s > 0.0) k = std::min(k, std::max(1, (int)(wait / step_s)));
+            else k = 1;
+        }
+        return std::max(1, k);
+    }
+
+    // One iteration: admit, advance every in-flight solve by the tick's
+    // steps (one graph replay each, one host synchronisation), retire.
     int tick(int* n_inflight)
     {
         int rc = admit(now());
         if (rc) return rc;
         if (!inflight.empty()) {
-            rc = batch.step(1);
+            const double t_start = now();
+            const int k = steps_this_tick(t_start);
+            rc = batch.step(k);
             if (rc) return rc;
             cudaError_t e = cudaStreamSynchronize(batch.stream);
             if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
-            for (long long id : inflight) reqs[id].remaining--;
-            ticks++;
-            inflight_sum += (double)inflight.size();
+            const double per = (now() - t_start) / k;
+            step_s = step_s > 0.0 ? 0.8 * step_s + 0.2 * per : per;
+            for (long long id : inflight) reqs[id].remaining -= k;
+            ticks += k;
+            inflight_sum += (double)inflight.size() * k;
             rc = retire(now());
             if (rc) return rc;
         }

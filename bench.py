@@ -459,8 +459,9 @@ def precision_form(a, cfg, dg, W, torch):
 
 
 def batched_form(a, dg, W, torch):
-    """Config 4: 256 uneven FP32 problems (N in 2..5) advanced together by one
-    persistent kernel per RK stage under a CUDA graph; autotuned tiles."""
+    """Config 4: 256 uneven FP32 problems (N in 2..5) advanced together by
+    persistent kernels per order, as parallel branches of a CUDA graph;
+    autotuned tiles."""
     cfgs = W.config4(seed=0, n=a.batch_instances)
     steps = max(1, min(a.batch_steps, 400))
     with dg.Batch(cfgs) as b:

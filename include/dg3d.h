@@ -253,8 +253,9 @@ int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_ele
  * Batched form (no counterpart in the reference, which runs one problem per
  * process): n independent problems of uneven element counts and orders
  * (ORDER 1..5), FP32 fields/fluxes/stages with the Kahan-compensated update,
- * advanced together by one persistent kernel per RK stage under a captured
- * CUDA graph.  Problem i takes its own dt[i] and stops after steps[i] steps;
+ * advanced together by persistent kernels per order (one group of problems
+ * per branch of a captured CUDA graph).  Problem i takes its own dt[i] and
+ * stops after steps[i] steps;
  * its exterior state is zero except the tone-burst source (whole face).
  * Each problem's result is independent of its batch-mates (bitwise).
  * ------------------------------------------------------------------------ */
@@ -293,7 +294,11 @@ double dg_serve_clock(const dg_server* s);
 int dg_serve_submit(dg_server* s, const dg_params* p, double dt, int steps, double arrival_time,
                     long long* id);
 /* One loop iteration: admit arrived requests that fit, advance every in-flight
- * solve one RK step, retire the finished ones. */
+ * solve by the same number of RK steps (one graph replay each, then one host
+ * synchronisation): as many as end no in-flight solve early and, while a
+ * request is still to arrive, as fit before its arrival by the running
+ * estimate of a step's time (at most 64; one while an arrived request waits
+ * for memory); then retire the finished ones. */
 int dg_serve_tick(dg_server* s, int* n_inflight);
 /* Run the loop in real time until every submitted request has finished. */
 int dg_serve_run(dg_server* s, double max_seconds);
