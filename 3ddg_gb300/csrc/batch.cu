@@ -1,7 +1,8 @@
 // Batched form (dg_batch_*): many independent FP32 problems of uneven
-// element counts and orders advanced together by the persistent stage kernel
-// of batch_kernels.cuh, one captured CUDA graph per RK step, tile sizes chosen
-// per order by an autotuner.  The serving form (serve.cu) drives the same
+// element counts and orders advanced together by the persistent stage kernels
+// of batch_kernels.cuh (one per order, each group of problems sharing an
+// operator on its own branch), one captured CUDA graph per RK step, tile sizes
+// chosen per order by an autotuner.  The serving form (serve.cu) drives the same
 // object, adding and removing problems as requests arrive and finish.
 #include <cuda_runtime.h>
 
