@@ -3,7 +3,8 @@ blocks), with a Gaussian pulse added to the tone burst so that every element
 carries data: one RK step against the C oracle (about 30 s of one host core),
 and size-independent properties over several steps: 2x2x2 blocks are bitwise
 one block, total mass is conserved with periodic boundaries, the FP32 form
-stays within its error bound."""
+stays within its error bound.  Config 4 at its full size (256 problems): the
+batched form agrees with the single-problem FP32 path."""
 import numpy as np
 import pytest
 
@@ -85,3 +86,28 @@ def test_full_size_fp32_within_tolerance(solver_for):
         s.close()
     p64, p32 = pressure(cfg, out[0]), pressure(cfg, out[1])
     assert np.linalg.norm(p32 - p64) <= 1e-5 * np.linalg.norm(p64)
+
+
+def test_full_size_batch_matches_single_problems():
+    """All 256 problems of config 4 (82.6 M nodes) advanced together; a sample
+    of each order agrees with the single-problem FP32 path (the batch applies
+    1/w after the line sums, so agreement is to rounding, not bitwise)."""
+    W = workloads()
+    m = dg()
+    cfgs = W.config4(seed=0)
+    steps = 20
+    with m.Batch(cfgs) as b:
+        b.step(steps)
+        picks = {}
+        for i, c in enumerate(cfgs):
+            picks.setdefault(c["ORDER"], i)
+        got = {i: b.state(i) for i in picks.values()}
+    assert len(picks) == 4
+    for i, (r, v) in got.items():
+        c = cfgs[i]
+        with m.Solver(c) as s:
+            s.step(c["DT"], steps)
+            r1, v1 = s.state()
+        assert np.max(np.abs(r1)) > 0
+        assert max_rel(pressure(c, r), pressure(c, r1)) <= 2e-5, (i, c["ORDER"])
+        assert max_rel(v, v1) <= 2e-5
