@@ -195,10 +195,31 @@ __host__ __device__ constexpr int axis_stride(int a)
 // Face nodes of an element, numbered t = (2 a + side) K^2 + fi for the faces
 // -X +X -Y +Y -Z +Z, fi = c[(a+1)%3] K + c[(a+2)%3]: the element's node on
 // the face (nf) and the neighbour's node across it (nn, in the neighbour).
+// The decoding is tabulated per order at compile time (one packed word per
+// face node: a 2 bits, side 1, fi 7, nf 10, nn 10), so that a thread loads its
+// face nodes' entries (coalesced) instead of redoing the integer arithmetic.
 template <int K>
-struct FaceNode {
+struct FaceTable {
+    int v[6 * K * K];
+    constexpr FaceTable() : v{}
+    {
+        constexpr int K2 = K * K;
+        for (int t = 0; t < 6 * K2; t++) {
+            const int a = t / (2 * K2), side = (t / K2) & 1, fi = t % K2, p = side ? K - 1 : 0;
+            const int nf = a == 0 ? p * K2 + fi : (a == 1 ? (fi % K) * K2 + p * K + fi / K : fi * K + p);
+            const int nn = nf + (side ? -(K - 1) : (K - 1)) * (a == 0 ? K2 : (a == 1 ? K : 1));
+            v[t] = a | (side << 2) | (fi << 3) | (nf << 10) | (nn << 20);
+        }
+    }
+};
+template <int K>
+__device__ const FaceTable<K> kFaceTable{};
+
+// The same decoding by integer arithmetic (no memory access).
+template <int K>
+struct FaceNodeArith {
     int a, side, fi, nf, nn;
-    __device__ __forceinline__ explicit FaceNode(int t)
+    __device__ __forceinline__ explicit FaceNodeArith(int t)
     {
         constexpr int K2 = K * K;
         a = t / (2 * K2);
@@ -207,6 +228,20 @@ struct FaceNode {
         const int p = side ? K - 1 : 0;
         nf = a == 0 ? p * K2 + fi : (a == 1 ? (fi % K) * K2 + p * K + fi / K : fi * K + p);
         nn = nf + (side ? -(K - 1) : (K - 1)) * axis_stride<K>(a);
+    }
+};
+
+template <int K>
+struct FaceNode {
+    int a, side, fi, nf, nn;
+    __device__ __forceinline__ explicit FaceNode(int t)
+    {
+        const int w = __ldg(&kFaceTable<K>.v[t]);
+        a = w & 3;
+        side = (w >> 2) & 1;
+        fi = (w >> 3) & 127;
+        nf = (w >> 10) & 1023;
+        nn = (w >> 20) & 1023;
     }
 };
 
