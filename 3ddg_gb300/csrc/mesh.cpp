@@ -14,8 +14,6 @@ std::string validate_params(const dg_params& p)
         if (p.num_blocks[a] < 1) return "NUM_BLOCKS must be >= 1";
         if (p.num_elements[a] < 1) return "NUM_ELEMENTS must be >= 1";
         if (!(p.elem_width[a] > 0.0)) return "ELEMENT_WIDTH must be > 0";
-        if (p.periodic[a] && (long long)p.num_blocks[a] * p.num_elements[a] < 2)
-            return "a periodic axis needs at least 2 elements";
     }
     if (!(p.rho0 > 0.0) || !(p.c0 > 0.0)) return "RHO0 and C0 must be > 0";
     for (int f = 0; f < 6; f++)

@@ -294,3 +294,23 @@ def test_fp32_every_order_within_tolerance(order, solver_for):
     p64, p32 = pressure(cfg, r64), pressure(cfg, r32)
     assert np.linalg.norm(p32 - p64) <= 1e-5 * np.linalg.norm(p64)
     assert np.linalg.norm(v32 - v64) <= 1e-5 * np.linalg.norm(v64)
+
+
+@pytest.mark.parametrize("ne,periodic,order", [((1, 1, 1), (0, 0, 0), 3), ((1, 2, 3), (1, 1, 1), 4),
+                                               ((2, 1, 1), (1, 0, 0), 4), ((1, 1, 2), (0, 0, 1), 5)])
+def test_tiny_meshes_match_oracle(ne, periodic, order, solver_for, oracle_for):
+    """One element along an axis: with a periodic axis the element is its own
+    neighbour across that axis (the reference's periodicSelf copies its own
+    opposite face).  FP64 against the oracle; FP32 against FP64."""
+    cfg = small(order=order, ne=ne, periodic=periodic)
+    cfg["EVALUATE_SPONGE"] = 0
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 4)
+    o.run(cfg["DT"], 4)
+    compare_state(cfg, s, o, STEP_TOL)
+    s32 = solver_for(dict(cfg, PRECISION=32))
+    s32.step(cfg["DT"], 4)
+    r64, _ = s.state()
+    r32, _ = s32.state()
+    p64, p32 = pressure(cfg, r64), pressure(cfg, r32)
+    assert np.linalg.norm(p32 - p64) <= 1e-5 * np.linalg.norm(p64)
