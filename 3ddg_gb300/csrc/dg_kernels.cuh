@@ -284,18 +284,64 @@ __device__ __forceinline__ int line_base(int t)
     return A == 0 ? t : (A == 1 ? (t % K) * K * K + t / K : t * K);
 }
 
-// One line of the LDG gradient along axis A.  A is a compile-time constant
-// so that the operator rows (kernel parameters) are constant-bank operands of
-// the FMAs rather than indexed constant loads.
+// Line owner with its own face terms (FP32, K >= 5): the two ends of line t
+// along axis A are the face nodes (A, 0, t) and (A, 1, t), so the owner
+// evaluates both numerical fluxes itself (neighbour values ro/uo/qo[side],
+// prefetched; own values from shared memory) and then the line sums.  The
+// face coefficients come from kernel parameters with a compile-time axis.
+template <int A, bool DIFF, typename T, int K, typename Smem>
+__device__ __forceinline__ void stage_line_faces(const OpConst<T, K>& Cv, Smem& S, int t, const T ro[2],
+                                                 const T uo[2], const T qo[2], int do_adv)
+{
+    constexpr int st = axis_stride<K>(A);
+    const int b0 = line_base<A, K>(t);
+    typename Pair<T>::type g[2];
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const int nf = b0 + (side ? (K - 1) * st : 0);
+        const T fm_s = S.f[A][nf].x, fa_s = S.m[A][nf];
+        T gm = T(0), gr = T(0);
+        if (do_adv) {
+            const T fmo = momentum_flux(ro[side], Cv.k1, Cv.k2);
+            const T fao = mass_flux(uo[side], ro[side], Cv.r0, Cv.linear_mass);
+            const T* cm = Cv.cM[A][side];
+            const T* cr = Cv.cA[A][side];
+            gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
+            gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
+        }
+        if (DIFF) gr += Cv.cQ[A][side] * (qo[side] + S.q[A][nf]);
+        g[side].x = gm;
+        g[side].y = gr;
+    }
+    typename Pair<T>::type v[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = S.f[A][b0 + j * st];
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        const T* row = Cv.rows[A][i];
+        T sm = row[K] * g[0].x, sr = row[K] * g[0].y;
+        sm += row[K + 1] * g[1].x;
+        sr += row[K + 1] * g[1].y;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            sm += row[j] * v[j].x;
+            sr += row[j] * v[j].y;
+        }
+        S.m[A][b0 + i * st] = sr;
+        S.q[A][b0 + i * st] = sm;
+    }
+}
+
+// The same for the LDG gradient: central flux of drho at both ends.
 template <int A, typename T, int K, typename Smem>
-__device__ __forceinline__ void grad_line(const OpConst<T, K>& Cv, Smem& S, int t)
+__device__ __forceinline__ void grad_line_faces(const OpConst<T, K>& Cv, Smem& S, int t, const T ro[2])
 {
     constexpr int st = axis_stride<K>(A);
     const int b0 = line_base<A, K>(t);
     T v[K];
 #pragma unroll
     for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
-    const T f0 = S.fl[A][0][t], fN = S.fl[A][1][t];
+    const T f0 = Cv.cQ[A][0] * (ro[0] + v[0]), fN = Cv.cQ[A][1] * (ro[1] + v[K - 1]);
 #pragma unroll
     for (int i = 0; i < K; i++) {
         const T* row = Cv.rows[A][i];
@@ -307,30 +353,32 @@ __device__ __forceinline__ void grad_line(const OpConst<T, K>& Cv, Smem& S, int 
     }
 }
 
-// One line of the stage operator along axis A: momentum and density sums of
-// the line's K outputs into S.q and S.m.
-template <int A, typename T, int K, typename Smem>
-__device__ __forceinline__ void stage_line(const OpConst<T, K>& Cv, Smem& S, int t)
+// Neighbour (or exterior) values of the two face nodes at the ends of line t
+// along axis a, for the line owners above: drho always, the normal velocity
+// with WITH_U, the gradient with WITH_Q (arrays not asked for are zeroed).
+template <bool INCR, bool WITH_U, bool WITH_Q, typename T, int K>
+__device__ __forceinline__ void line_end_values(const StageIO<T>& io, const MeshDev<T>& m,
+                                                const OpConst<T, K>& C, int e, int a, int t, T ro[2], T uo[2],
+                                                T qo[2])
 {
-    constexpr int st = axis_stride<K>(A);
-    const int b0 = line_base<A, K>(t);
-    typename Pair<T>::type v[K];
+    const int st = axis_stride<K>(a);
+    const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K * K + t / K : t * K);
 #pragma unroll
-    for (int j = 0; j < K; j++) v[j] = S.f[A][b0 + j * st];
-    const typename Pair<T>::type g0 = S.g[A][0][t], gN = S.g[A][1][t];
-#pragma unroll
-    for (int i = 0; i < K; i++) {
-        const T* row = Cv.rows[A][i];
-        T sm = row[K] * g0.x, sr = row[K] * g0.y;
-        sm += row[K + 1] * gN.x;
-        sr += row[K + 1] * gN.y;
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-            sm += row[j] * v[j].x;
-            sr += row[j] * v[j].y;
+    for (int side = 0; side < 2; side++) {
+        ro[side] = T(0);
+        uo[side] = T(0);
+        qo[side] = T(0);
+        const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * a + side);
+        if (code >= 0) {
+            const size_t o2 = (size_t)code * io.np + b0 + (side ? 0 : (K - 1) * st);
+            ro[side] = load_in<INCR>(io, 0, o2);
+            if (WITH_U) uo[side] = load_in<INCR>(io, 1 + a, o2);
+            if (WITH_Q) qo[side] = __ldg(io.q + (size_t)a * io.fs + o2);
+        } else {
+            T u2;
+            exterior<T, K>(m, C, -1 - code, side, t, ro[side], u2);
+            if (WITH_U) uo[side] = u2;
         }
-        S.m[A][b0 + i * st] = sr;
-        S.q[A][b0 + i * st] = sm;
     }
 }
 
@@ -359,6 +407,27 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     const bool live = e < m.n_elem;
     const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
+    if constexpr (LINES) {
+        // Line owners with their own face terms: one barrier per element.
+        constexpr int WPA = (K2 + 31) / 32;
+        const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
+        const bool owner = live && a < 3 && t < K2;
+        T rho = T(0), ro[2] = {T(0), T(0)}, unused_u[2], unused_q[2];
+        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
+        if (owner) line_end_values<INCR, false, false, T, K>(io, m, C, e, a, t, ro, unused_u, unused_q);
+        S.r[n] = rho;
+        __syncthreads();
+        if (owner) {
+            if (a == 0) grad_line_faces<0>(Cv, S, t, ro);
+            else if (a == 1) grad_line_faces<1>(Cv, S, t, ro);
+            else grad_line_faces<2>(Cv, S, t, ro);
+        }
+        __syncthreads();
+        if (!act) return;
+#pragma unroll
+        for (int a2 = 0; a2 < 3; a2++) io.q_out[(size_t)a2 * io.fs + (size_t)e * io.np + n] = S.out[a2][n];
+        return;
+    }
     // Face nodes assigned densely (see stage_kernel): their neighbour (or
     // exterior) values are loaded with the thread's own node.
     int code[R];
@@ -399,20 +468,6 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         S.fl[F.a][F.side][F.fi] = C.cQ[F.a][F.side] * (ro[r] + S.r[F.nf]);
     }
     __syncthreads();
-    if constexpr (LINES) {
-        constexpr int WPA = (K2 + 31) / 32;
-        const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
-        if (live && a < 3 && t < K2) {
-            if (a == 0) grad_line<0>(Cv, S, t);
-            else if (a == 1) grad_line<1>(Cv, S, t);
-            else grad_line<2>(Cv, S, t);
-        }
-        __syncthreads();
-        if (!act) return;
-#pragma unroll
-        for (int a2 = 0; a2 < 3; a2++) io.q_out[(size_t)a2 * io.fs + (size_t)e * io.np + n] = S.out[a2][n];
-        return;
-    }
     if (!act) return;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -591,6 +646,7 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
 {
     constexpr bool LINES = K >= 5;  // three warp-groups of ceil(K^2 / 32) warps fit in NPT
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
+    constexpr int WPA = (K2 + 31) / 32;
     __shared__ PlainSmem<T, K> sm_all[epb_of(K)];
     PlainSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
@@ -600,15 +656,20 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
     const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const size_t off = (size_t)e * io.np + n;
+    // line owner (LINES): warp group a, line t of that axis
+    const int la = n / 32 / WPA, lt = (n / 32 % WPA) * 32 + n % 32;
+    const bool owner = LINES && live && la < 3 && lt < K2;
 
     int code[R];
+    if constexpr (!LINES) {
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = n + r * NPT;
-        code[r] = 0;
-        if (live && t < NF) {
-            const FaceNode<K> F(t);
-            code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            code[r] = 0;
+            if (live && t < NF) {
+                const FaceNode<K> F(t);
+                code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+            }
         }
     }
     const T sig = (act && do_sponge) ? __ldg(m.sigma + e) : T(0);
@@ -625,20 +686,26 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
     }
-    T ro[R], uo[R], qo[R];
+    // Neighbour (or exterior) values: of the two ends of the owned line
+    // (LINES), else of the densely assigned face nodes.
+    T ro[R > 2 ? R : 2], uo[R > 2 ? R : 2], qo[R > 2 ? R : 2];
+    if constexpr (LINES) {
+        if (owner) line_end_values<true, true, DIFF, T, K>(io, m, C, e, la, lt, ro, uo, qo);
+    } else {
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        ro[r] = uo[r] = qo[r] = T(0);
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        if (code[r] >= 0) {
-            const size_t o2 = (size_t)code[r] * io.np + F.nn;
-            ro[r] = load_in<true>(io, 0, o2);
-            uo[r] = load_in<true>(io, 1 + F.a, o2);
-            if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
-        } else {
-            exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo[r]);
+        for (int r = 0; r < R; r++) {
+            ro[r] = uo[r] = qo[r] = T(0);
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            if (code[r] >= 0) {
+                const size_t o2 = (size_t)code[r] * io.np + F.nn;
+                ro[r] = load_in<true>(io, 0, o2);
+                uo[r] = load_in<true>(io, 1 + F.a, o2);
+                if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
+            } else {
+                exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo[r]);
+            }
         }
     }
     OpRows<T, K> R_;
@@ -660,37 +727,16 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
         if (DIFF) S.q[a][n] = q[a];
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
-        T gm = T(0), gr = T(0);
-        if (do_adv) {
-            const T fmo = momentum_flux(ro[r], C.k1, C.k2);
-            const T fao = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
-            const T* cm = C.cM[F.a][F.side];
-            const T* cr = C.cA[F.a][F.side];
-            gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
-            gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
-        }
-        if (DIFF) gr += C.cQ[F.a][F.side] * (qo[r] + S.q[F.a][F.nf]);
-        S.g[F.a][F.side][F.fi].x = gm;
-        S.g[F.a][F.side][F.fi].y = gr;
-    }
-    __syncthreads();
 
     T r[4] = {T(0), T(0), T(0), T(0)};
     if constexpr (LINES) {
-        // Line owners; the per-axis results reuse S.m (density) and S.q
-        // (momentum), whose last readers were the face terms before the barrier.
-        constexpr int WPA = (K2 + 31) / 32;
-        const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
-        if (live && a < 3 && t < K2) {
-            if (a == 0) stage_line<0>(Cv, S, t);
-            else if (a == 1) stage_line<1>(Cv, S, t);
-            else stage_line<2>(Cv, S, t);
+        // Line owners evaluate the face terms at both ends of their line and
+        // the line sums; the per-axis results reuse S.m (density) and S.q
+        // (momentum) of the owner's own line nodes, read before written.
+        if (owner) {
+            if (la == 0) stage_line_faces<0, DIFF>(Cv, S, lt, ro, uo, qo, do_adv);
+            else if (la == 1) stage_line_faces<1, DIFF>(Cv, S, lt, ro, uo, qo, do_adv);
+            else stage_line_faces<2, DIFF>(Cv, S, lt, ro, uo, qo, do_adv);
         }
         __syncthreads();
         if (!act) return;
@@ -700,6 +746,26 @@ incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__
             r[1 + a2] = do_adv ? S.q[a2][n] : T(0);
         }
     } else {
+#pragma unroll
+        for (int rr = 0; rr < R; rr++) {
+            const int t = n + rr * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
+            T gm = T(0), gr = T(0);
+            if (do_adv) {
+                const T fmo = momentum_flux(ro[rr], C.k1, C.k2);
+                const T fao = mass_flux(uo[rr], ro[rr], C.r0, C.linear_mass);
+                const T* cm = C.cM[F.a][F.side];
+                const T* cr = C.cA[F.a][F.side];
+                gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
+                gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
+            }
+            if (DIFF) gr += C.cQ[F.a][F.side] * (qo[rr] + S.q[F.a][F.nf]);
+            S.g[F.a][F.side][F.fi].x = gm;
+            S.g[F.a][F.side][F.fi].y = gr;
+        }
+        __syncthreads();
         if (!act) return;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
