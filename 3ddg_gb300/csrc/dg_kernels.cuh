@@ -4,7 +4,8 @@
 //   ldg_gradient_kernel  G_a = -D_c d(drho)/dx_a by LDG with the central flux
 //                        (Element::OperateQFromDRho, cppsrc/Element.cpp:623-690;
 //                        stored pre-multiplied by -D_c, the diffusive flux)
-//   stage_kernel         volume + face terms of the advection operator
+//   stage_kernel (FP64), incr_stage_kernel (FP32 increment form)
+//                        volume + face terms of the advection operator
 //                        (Element::OperateUFromV, cppsrc/Element.cpp:475-620),
 //                        LDG divergence (Element::OperateDRhoFromQ, :691-758),
 //                        sponge (Element::OperateSponge, :760-781) and the RK
@@ -12,20 +13,28 @@
 //                        fused into one pass over the state.
 //
 // Mapping: one thread per node, one warp-aligned slice of NPT threads per
-// element, EPB elements per CTA.  Each element stages its volume fluxes and
-// its face fluxes in shared memory; the line sums along each axis read shared
-// memory with the operator rows held in registers.  The reference's per-line
-// QR solve of (M q w) x = S q f - F becomes
+// element, EPB elements per CTA.  Each thread loads its node (and the
+// neighbour values its face work needs) before the first use; the element
+// stages its volume fluxes in shared memory; face fluxes and line sums follow
+// after barriers.  The reference's per-line QR solve of
+// (M q w) x = S q f - F becomes
 //     x = (1/w) D f - (1/(q w)) (M^-1 e_0 F_0 + M^-1 e_N F_N),  D = M^-1 S,
 // with D and the lift columns computed once on the host in FP64.
 //
-// The FP64 path is bound by the FP64 pipe, so every constant factor is folded
-// on the host into the per-launch operator (OpConst): the RK stage weight ca,
-// 1/w_a and the equations' lift scales go into per-axis copies of D and into
-// the face-flux coefficients, the gradient carries -D_c so that the LDG
+// FP64 (bound by the FP64 pipe): every constant factor is folded on the host
+// into the per-launch operator (OpConst): the RK stage weight ca, 1/w_a and
+// the equations' lift scales go into per-axis copies of D and into the
+// face-flux coefficients, the gradient carries -D_c so that the LDG
 // divergence and the mass-flux divergence share one line sum, and the sponge
-// folds into the RK combination.  Per node and stage each axis then costs
-// 2 (K + 2) FMAs for the volume and lift terms.
+// folds into the RK combination.  Per node and stage each axis costs
+// 2 (K + 2) FMAs for the volume and lift terms; the element's face nodes are
+// dealt out densely to its threads so that no warp issues face arithmetic for
+// lanes that have none.
+//
+// FP32 (bound by the L1 data pipe, load latency and issue): for K >= 5 line
+// owners (a warp per axis, a lane per line) evaluate their line's two face
+// terms and its K outputs with the operator as kernel parameters, instead of
+// every node summing its own three lines from shared memory.
 //
 // Neighbour face values are read straight from the neighbour element (same
 // block or another block of the same HBM pool) through the face table, which
@@ -141,15 +150,6 @@ struct Pair<float> {
 template <>
 struct Pair<double> {
     using type = double2;
-};
-
-// Per element: for each axis a, the pair (f_mom, f_mass along a + G_a) of every
-// node, and the pair (momentum, density) of every face term, so each step of a
-// line sum is one 8- or 16-byte shared-memory load feeding two FMAs.
-template <typename T, int K>
-struct StageSmem {
-    typename Pair<T>::type f[3][npt_of(K)];
-    typename Pair<T>::type g[3][2][K * K];  // [axis][side][face node]
 };
 
 template <typename T, int K>
@@ -484,9 +484,11 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     }
 }
 
-// Shared memory of the plain stage kernel: the line-sum operands (f, g as in
-// StageSmem) and each node's own mass flux and gradient, which the face phase
-// reads.
+// Shared memory of a stage kernel, per element: for each axis a, the pair
+// (f_mom, f_mass along a + G_a) of every node (one 8- or 16-byte load feeds
+// two FMAs of a line sum), the pair (momentum, density) of every face term
+// [axis][side][face node], and each node's own mass flux and gradient, which
+// the face phase reads (and the line owners then reuse for their results).
 template <typename T, int K>
 struct PlainSmem {
     typename Pair<T>::type f[3][npt_of(K)];
@@ -991,19 +993,5 @@ __global__ void pack_grid_kernel(const T* __restrict__ state, size_t fs, int np,
     }
 }
 
-template <typename T>
-__global__ void unpack_grid_kernel(T* __restrict__ state, size_t fs, int np, int nfields,
-                                   GridMap g, int n_elem, const double* __restrict__ in, size_t gsize)
-{
-    const int K3 = g.K * g.K * g.K;
-    const long long total = (long long)n_elem * K3;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int e = (int)(i / K3), n = (int)(i % K3);
-        const size_t gi = grid_index(g, e, n);
-        for (int f = 0; f < nfields; f++)
-            state[(size_t)f * fs + (size_t)e * np + n] = (T)in[(size_t)f * gsize + gi];
-    }
-}
 
 }  // namespace dg
