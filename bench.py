@@ -170,7 +170,7 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-FP64_PEAK_TFLOPS = 1.19  # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_fp32_peak_probe.md)
+FP64_PEAK_TFLOPS = 1.19  # FP64 FMA throughput measured on a GB300 (profiles/fp64_fp32_peak_probe.md)
 
 
 def profiled_traffic(kind: str):

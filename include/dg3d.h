@@ -239,7 +239,8 @@ int dg_stream(dg_handle* h, void** stream);
  * stream and returns, per kernel kind k (0 = stage kernel, 1 = LDG gradient),
  * the number of launches, their summed event time in ms, and their summed
  * algorithmic DRAM bytes and FP flops (the data each launch must move once and
- * the arithmetic it must do, as counted in the design doc). */
+ * the arithmetic it must do: per node, the fields read and written once, and
+ * 2 flops per FMA of the line sums, face fluxes and stage combination). */
 int dg_profile(dg_handle* h, int enable);
 int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double* bytes,
                     double* flops);
