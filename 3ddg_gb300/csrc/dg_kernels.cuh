@@ -641,8 +641,16 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 // (``Cv``; warp-uniform indices, so constant-bank operands).  The per-axis
 // results go to shared memory and each node thread adds them up.
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM asked of the compiler for the FP32 stage kernel (0: no
+// request): at K = 5 it fits 40 registers without spilling, 12 CTAs per SM.
+template <typename T, int K>
+__host__ __device__ constexpr int incr_min_blocks()
+{
+    return (sizeof(T) == 4 && K == 5) ? 12 : 0;
+}
+
 template <typename T, int K, bool DIFF>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (incr_min_blocks<T, K>()))
 incr_stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, const OpConst<T, K> Cv,
                   int do_adv, int do_sponge)
 {
