@@ -316,11 +316,12 @@ __host__ __device__ constexpr size_t batch_smem_bytes()
 }
 
 // Resident CTAs per SM asked of the compiler for order K (register budget
-// 65536 / (256 x blocks)): the most that each order's path fits without
-// spilling (K = 2 in 48 registers, K = 4 in 40, the others in 64).
+// 65536 / (256 x blocks)), chosen by measurement on config 4: 5 (48
+// registers) for K = 2, 4, 6 (no spills at K = 2, 4; 20 bytes at K = 6), 4 (64
+// registers) for K = 3, 5, which spill heavily at 48.
 __host__ __device__ constexpr int batch_min_blocks(int K)
 {
-    return K == 2 ? 5 : (K == 4 ? 6 : 4);
+    return K == 2 || K == 4 || K == 6 ? 5 : 4;
 }
 
 __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProblem* src)
