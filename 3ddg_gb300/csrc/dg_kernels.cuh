@@ -73,7 +73,8 @@ __host__ __device__ constexpr int oprow_len()
 //   stage kernel:    D[a] = ca D / w_a;   cM, cA: face coefficients of the
 //                    momentum / mass equations times ca * (lift scale);
 //                    cQ[a] = (+0.5, -0.5) ca / w_a (central flux of G).
-//   gradient kernel: D[a] = D_c D / w_a;  cQ[a] = (+0.5, -0.5) D_c / w_a.
+//   gradient kernel: D[a] = D_c D / w_a;  lift columns times the central-flux
+//                    factors (+0.5, -0.5) D_c / w_a (cQ unused).
 // rows[a][i] = (D[a][i][0..K-1], L0[i], LN[i], 0...) with the lift columns
 // L0 = M^-1 e_0, LN = M^-1 e_N, so that a thread loads its row of each axis
 // with one or two 16-byte loads.
@@ -122,6 +123,7 @@ struct StageIO {
     T* comp;
     const T* q;            // LDG gradient (times -D_c), 3 fields
     T* q_out;              // gradient kernel output
+    const T* elem_b;       // PLAIN: cb - ca sigma per element for this stage (null: from sigma)
     size_t fs;             // field stride (n_elem * NP)
     int np;                // nodes per element in memory
     T ca, cb, cc, eps;
@@ -341,7 +343,7 @@ __device__ __forceinline__ void grad_line_faces(const OpConst<T, K>& Cv, Smem& S
     T v[K];
 #pragma unroll
     for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
-    const T f0 = Cv.cQ[A][0] * (ro[0] + v[0]), fN = Cv.cQ[A][1] * (ro[1] + v[K - 1]);
+    const T f0 = ro[0] + v[0], fN = ro[1] + v[K - 1];  // flux factors are in the lift columns
 #pragma unroll
     for (int i = 0; i < K; i++) {
         const T* row = Cv.rows[A][i];
@@ -465,7 +467,7 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         const int t = n + r * NPT;
         if (!live || t >= NF) continue;
         const FaceNode<K> F(t);
-        S.fl[F.a][F.side][F.fi] = C.cQ[F.a][F.side] * (ro[r] + S.r[F.nf]);
+        S.fl[F.a][F.side][F.fi] = ro[r] + S.r[F.nf];  // flux factors are in the lift columns
     }
     __syncthreads();
     if (!act) return;
@@ -508,8 +510,16 @@ struct PlainSmem {
 // since almost every warp holds some node on each face pair.)  The
 // neighbour values of those face nodes are loaded with the thread's own node.
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM asked of the compiler for the FP64 stage kernel (0:
+// no request): at K = 5, 64 registers keep 8 CTAs (32 warps) per SM.
+template <typename T, int K>
+__host__ __device__ constexpr int plain_min_blocks()
+{
+    return (sizeof(T) == 8 && K == 5) ? 8 : 0;
+}
+
 template <typename T, int K, bool DIFF>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K))
+__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (plain_min_blocks<T, K>()))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
@@ -592,29 +602,33 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     __syncthreads();
     if (!act) return;
 
+    // The density equation is one FMA chain through the three axes (no
+    // per-axis partial sums to add): the kernel is bound by FP64 issue, so
+    // every FP64 instruction saved per node counts.
     T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int st = axis_stride<K>(a), base = n - c[a] * st;
         const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
         const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-        T sm = R_.l0[a] * g0.x, sr = R_.l0[a] * g0.y;
+        T sm = R_.l0[a] * g0.x;
         sm += R_.ln[a] * gN.x;
-        sr += R_.ln[a] * gN.y;
+        r_rho += R_.l0[a] * g0.y;
+        r_rho += R_.ln[a] * gN.y;
 #pragma unroll
         for (int j = 0; j < K; j++) {
             const typename Pair<T>::type v = S.f[a][base + j * st];
             sm += R_.d[a][j] * v.x;
-            sr += R_.d[a][j] * v.y;
+            r_rho += R_.d[a][j] * v.y;
         }
-        r_rho += sr;
         r_u[a] = do_adv ? sm : T(0);
     }
-    const T ks = do_sponge ? io.ca * __ldg(m.sigma + e) : T(0);
+    // cb - ca sigma of this element: tabulated per stage by the host, so that
+    // no thread spends FP64 instructions on it; computed here when absent.
+    const T cbe = io.elem_b ? __ldg(io.elem_b + e) : io.cb - (do_sponge ? io.ca * __ldg(m.sigma + e) : T(0));
 
     const T r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
     const T s4[4] = {rho, u[0], u[1], u[2]};
-    const T cbe = io.cb - ks;
 #pragma unroll
     for (int f = 0; f < 4; f++) {
         const size_t o = (size_t)f * io.fs + off;
@@ -876,13 +890,15 @@ inline OpConst<T, K> make_grad_const(const double* deriv, const double* lift0, c
 {
     OpConst<T, K> C{};
     for (int a = 0; a < 3; a++) {
+        // central flux of drho, (+0.5, -0.5) D_c / w_a, folded into the lift
+        // columns: the kernels lift the plain face sum (own + other)
+        const double q0 = 0.5 * diff_const / w[a], qN = -0.5 * diff_const / w[a];
         for (int i = 0; i < K; i++) {
             for (int j = 0; j < K; j++) C.rows[a][i][j] = (T)(diff_const * deriv[i * K + j] / w[a]);
-            C.rows[a][i][K] = (T)lift0[i];
-            C.rows[a][i][K + 1] = (T)liftN[i];
+            C.rows[a][i][K] = (T)(lift0[i] * q0);
+            C.rows[a][i][K + 1] = (T)(liftN[i] * qN);
         }
-        C.cQ[a][0] = (T)(0.5 * diff_const / w[a]);
-        C.cQ[a][1] = (T)(-0.5 * diff_const / w[a]);
+        C.cQ[a][0] = C.cQ[a][1] = T(1);
     }
     C.inv_c2 = (T)(1.0 / (c0 * c0));
     C.inv_z = (T)(1.0 / (rho0 * c0));

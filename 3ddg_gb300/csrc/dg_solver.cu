@@ -170,9 +170,34 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slo
     s.launches++;
 }
 
+// FP64 plain form: the stage input's weight with the sponge folded in,
+// cb - ca sigma_e, per element for each of the three RK stages (stage-major),
+// so that the stage kernel reads it instead of computing it at every node.
+int upload_elem_weights(Solver& s, double dt)
+{
+    const size_t ne = (size_t)s.mesh.n_elem;
+    const double w23 = s.p.rk_exact ? 2.0 / 3.0 : (double)(2.0f / 3.0f);
+    const double ca[3] = {dt, dt * .25, dt * 2.0 / 3.0}, cb[3] = {1.0, .25, w23};
+    std::vector<double>& h = s.h_elem_b;
+    h.resize(3 * ne);
+    for (int k = 0; k < 3; k++)
+        for (size_t e = 0; e < ne; e++) h[k * ne + e] = s.p.eval_sponge ? cb[k] - ca[k] * s.mesh.sigma[e] : cb[k];
+    if (!s.d_elem_b) {
+        cudaError_t e = cudaMalloc(&s.d_elem_b, h.size() * sizeof(double));
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    cudaError_t e = cudaMemcpyAsync(s.d_elem_b, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s.stream);
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    return DG_OK;
+}
+
 template <typename T>
 int upload_consts(Solver& s, double dt)
 {
+    if constexpr (sizeof(T) == 8) {
+        int rc = upload_elem_weights(s, dt);
+        if (rc) return rc;
+    }
     switch (s.mesh.K) {
     case 2: return upload_consts_k<T, 2>(s, dt);
     case 3: return upload_consts_k<T, 3>(s, dt);
@@ -289,6 +314,7 @@ int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
         int rc = upload_consts<double>(*this, dt);
         if (rc) return rc;
     }
+    if (!rhs_only) io.elem_b = d_elem_b + (size_t)s_idx * mesh.n_elem;
     if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
     dispatch_stage<double, false>(*this, io, md, rhs_only ? 4 : s_idx);
     return DG_OK;
@@ -740,6 +766,7 @@ Solver::~Solver()
     if (d_bnd_ap) cudaFree(d_bnd_ap);
     if (d_bnd_src) cudaFree(d_bnd_src);
     if (d_const) cudaFree(d_const);
+    if (d_elem_b) cudaFree(d_elem_b);
     if (d_probe_off) cudaFree(d_probe_off);
     if (d_probe_rec) cudaFree(d_probe_rec);
     if (stream) cudaStreamDestroy(stream);

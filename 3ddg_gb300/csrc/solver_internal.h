@@ -37,6 +37,8 @@ struct Solver {
     int* d_bnd_src = nullptr;
     void* d_const = nullptr;  // per-launch operators: 3 RK stages, LDG gradient, bare RHS
     std::vector<char> h_const;  // host copy of d_const (for by-value kernel parameters)
+    double* d_elem_b = nullptr;  // FP64: cb - ca sigma per element for the 3 RK stages
+    std::vector<double> h_elem_b;
     double const_dt = 0.0;
     int cur = 0;
     bool ic_live = false;
