@@ -124,6 +124,8 @@ struct StageIO {
     const T* q;            // LDG gradient (times -D_c), 3 fields
     T* q_out;              // gradient kernel output
     const T* elem_b;       // PLAIN: cb - ca sigma per element for this stage (null: from sigma)
+    const T* flux_in;      // PLAIN, flux mode 2: volume fluxes of src (f_mom, f_mass x, y, z)
+    T* flux_out;           // PLAIN, flux modes 1, 2: the same of dst
     size_t fs;             // field stride (n_elem * NP)
     int np;                // nodes per element in memory
     T ca, cb, cc, eps;
@@ -518,7 +520,17 @@ __host__ __device__ constexpr int plain_min_blocks()
     return (sizeof(T) == 8 && K == 5) ? 8 : 0;
 }
 
-template <typename T, int K, bool DIFF>
+//
+// Flux modes (FLUX; 1 and 2 only with advection on):
+//   0: the volume fluxes of the element's nodes and of its face neighbours'
+//      nodes are evaluated from the state;
+//   1: as 0, and the fluxes of the output state are written to flux_out;
+//   2: both are read from flux_in (the fluxes of src, written by the stage
+//      that produced it) and those of the output are written to flux_out.
+// Mode 2 trades 64 bytes of HBM traffic per node for the FP64 instructions
+// of evaluating every interior face node's neighbour flux a second time
+// (its own element evaluates it for its line sums).
+template <typename T, int K, bool DIFF, int FLUX>
 __global__ void __launch_bounds__(npt_of(K) * epb_of(K), (plain_min_blocks<T, K>()))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
 {
@@ -536,15 +548,22 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     R_.load(C, c, act);
 
     T rho = T(0), u[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
+    T fl[4] = {T(0), T(0), T(0), T(0)};
     if (act) {
-        rho = load_in<false>(io, 0, off);
+        if (FLUX != 2) {  // mode 2 needs the state only for the stage combination
+            rho = load_in<false>(io, 0, off);
 #pragma unroll
-        for (int a = 0; a < 3; a++) u[a] = load_in<false>(io, 1 + a, off);
+            for (int a = 0; a < 3; a++) u[a] = load_in<false>(io, 1 + a, off);
+        }
         if (DIFF)
 #pragma unroll
             for (int a = 0; a < 3; a++) q[a] = __ldg(io.q + (size_t)a * io.fs + off);
+        if (FLUX == 2)
+#pragma unroll
+            for (int f = 0; f < 4; f++) fl[f] = __ldg(io.flux_in + (size_t)f * io.fs + off);
     }
-    // Neighbour (or exterior) values of this thread's face nodes.
+    // Neighbour (or exterior) values of this thread's face nodes: drho and
+    // the normal velocity, or in flux mode 2 their momentum and mass fluxes.
     T ro[R], uo[R], qo[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -555,16 +574,30 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
         const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
         if (code >= 0) {
             const size_t o2 = (size_t)code * io.np + F.nn;
-            ro[r] = load_in<false>(io, 0, o2);
-            uo[r] = load_in<false>(io, 1 + F.a, o2);
+            if (FLUX == 2) {
+                ro[r] = __ldg(io.flux_in + o2);
+                uo[r] = __ldg(io.flux_in + (size_t)(1 + F.a) * io.fs + o2);
+            } else {
+                ro[r] = load_in<false>(io, 0, o2);
+                uo[r] = load_in<false>(io, 1 + F.a, o2);
+            }
             if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
         } else {
             exterior<T, K>(m, C, -1 - code, F.side, F.fi, ro[r], uo[r]);
+            if (FLUX == 2) {
+                const T fm = momentum_flux(ro[r], C.k1, C.k2);
+                uo[r] = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
+                ro[r] = fm;
+            }
         }
     }
 
     T fmom = T(0), fmass[3] = {T(0), T(0), T(0)};
-    if (do_adv) {
+    if (FLUX == 2) {
+        fmom = fl[0];
+#pragma unroll
+        for (int a = 0; a < 3; a++) fmass[a] = fl[1 + a];
+    } else if (do_adv) {
         fmom = momentum_flux(rho, C.k1, C.k2);
 #pragma unroll
         for (int a = 0; a < 3; a++) fmass[a] = mass_flux(u[a], rho, C.r0, C.linear_mass);
@@ -588,8 +621,8 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
         const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
         T gm = T(0), gr = T(0);
         if (do_adv) {
-            const T fmo = momentum_flux(ro[r], C.k1, C.k2);
-            const T fao = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
+            const T fmo = FLUX == 2 ? ro[r] : momentum_flux(ro[r], C.k1, C.k2);
+            const T fao = FLUX == 2 ? uo[r] : mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
             const T* cm = C.cM[F.a][F.side];
             const T* cr = C.cA[F.a][F.side];
             gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
@@ -626,15 +659,29 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     // cb - ca sigma of this element: tabulated per stage by the host, so that
     // no thread spends FP64 instructions on it; computed here when absent.
     const T cbe = io.elem_b ? __ldg(io.elem_b + e) : io.cb - (do_sponge ? io.ca * __ldg(m.sigma + e) : T(0));
+    if (FLUX == 2) {
+        rho = load_in<false>(io, 0, off);
+#pragma unroll
+        for (int a = 0; a < 3; a++) u[a] = load_in<false>(io, 1 + a, off);
+    }
 
     const T r[4] = {r_rho, r_u[0], r_u[1], r_u[2]};
     const T s4[4] = {rho, u[0], u[1], u[2]};
+    T vo[4];
 #pragma unroll
     for (int f = 0; f < 4; f++) {
         const size_t o = (size_t)f * io.fs + off;
         T v = r[f] + s4[f] * cbe;
         if (io.old) v += io.old[o] * io.cc;
         io.dst[o] = v;
+        vo[f] = v;
+    }
+    if (FLUX >= 1) {
+        // the next stage's fluxes, evaluated as that stage would from dst
+        io.flux_out[off] = momentum_flux(vo[0], C.k1, C.k2);
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            io.flux_out[(size_t)(1 + a) * io.fs + off] = mass_flux(vo[1 + a], vo[0], C.r0, C.linear_mass);
     }
 }
 

@@ -144,6 +144,18 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
     s.launches++;
 }
 
+// FP64 stage kernel in the flux mode that io asks for (flux_out: write the
+// output's volume fluxes; flux_in: read the input's).
+template <typename T, int K, bool DIFF>
+void launch_plain(const Solver& s, dim3 grid, dim3 block, const StageIO<T>& io, const MeshDev<T>& md,
+                  const OpConst<T, K>* Cp)
+{
+    const int adv = s.p.eval_advect, sp = s.p.eval_sponge;
+    if (io.flux_out && io.flux_in) stage_kernel<T, K, DIFF, 2><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
+    else if (io.flux_out) stage_kernel<T, K, DIFF, 1><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
+    else stage_kernel<T, K, DIFF, 0><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
+}
+
 template <typename T, int K, bool INCR>
 void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slot)
 {
@@ -161,10 +173,8 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slo
             incr_stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, Cv, s.p.eval_advect,
                                                                         s.p.eval_sponge);
     } else {
-        if (s.p.eval_diff)
-            stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
-        else
-            stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, s.p.eval_advect, s.p.eval_sponge);
+        if (s.p.eval_diff) launch_plain<T, K, true>(s, grid, block, io, md, Cp);
+        else launch_plain<T, K, false>(s, grid, block, io, md, Cp);
     }
     s.prof_end(0, ev, stage_bytes<T, INCR>(s, io), stage_flops(s, io.old != nullptr || io.inc != nullptr));
     s.launches++;
@@ -314,9 +324,18 @@ int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
         int rc = upload_consts<double>(*this, dt);
         if (rc) return rc;
     }
+    const bool fluxes = !rhs_only && d_flux[0];
     if (!rhs_only) io.elem_b = d_elem_b + (size_t)s_idx * mesh.n_elem;
+    if (fluxes) {
+        io.flux_in = flux_valid ? d_flux[flux_cur] : nullptr;
+        io.flux_out = d_flux[1 - flux_cur];
+    }
     if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
     dispatch_stage<double, false>(*this, io, md, rhs_only ? 4 : s_idx);
+    if (fluxes) {
+        flux_cur = 1 - flux_cur;
+        flux_valid = true;
+    }
     return DG_OK;
 }
 
@@ -542,6 +561,7 @@ int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_devi
     launches++;
     DG_CUDA(cudaGetLastError());
     if (!fp64()) DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
+    flux_valid = false;
     ic_live = false;
     return DG_OK;
 }
@@ -630,6 +650,7 @@ size_t Solver::device_bytes() const
     const size_t es = fp64() ? 8 : 4;
     size_t nbuf = fp64() ? 3 : 5;  // FP64: U, k1, k2; FP32: u0, u1, comp, d1, d2
     size_t bytes = nbuf * 4 * fs * es + 3 * fs * es;
+    if (fp64() && p.eval_advect) bytes += 2 * 4 * fs * es;  // volume-flux buffers
     bytes += (size_t)mesh.n_elem * 6 * sizeof(int) + (size_t)mesh.n_elem * es;
     bytes += (size_t)mesh.n_bnd * (3 * mesh.K * mesh.K * es + sizeof(int));
     return bytes;
@@ -663,6 +684,9 @@ int Solver::init(const dg_params& prm, const char* matrix_file, const char* coef
         DG_CUDA(cudaMemsetAsync(buf[i], 0, 4 * fs * es, stream));
     }
     DG_CUDA(cudaMalloc(&qbuf, 3 * fs * es));
+    if (fp64() && p.eval_advect)
+        for (double*& f : d_flux) DG_CUDA(cudaMalloc(&f, 4 * fs * es));
+    flux_valid = false;
     DG_CUDA(cudaMemsetAsync(qbuf, 0, 3 * fs * es, stream));
     DG_CUDA(cudaMalloc(&d_nbr, mesh.nbr.size() * sizeof(int)));
     DG_CUDA(cudaMemcpy(d_nbr, mesh.nbr.data(), mesh.nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -767,6 +791,8 @@ Solver::~Solver()
     if (d_bnd_src) cudaFree(d_bnd_src);
     if (d_const) cudaFree(d_const);
     if (d_elem_b) cudaFree(d_elem_b);
+    for (double* f : d_flux)
+        if (f) cudaFree(f);
     if (d_probe_off) cudaFree(d_probe_off);
     if (d_probe_rec) cudaFree(d_probe_rec);
     if (stream) cudaStreamDestroy(stream);

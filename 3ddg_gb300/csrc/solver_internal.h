@@ -38,6 +38,12 @@ struct Solver {
     void* d_const = nullptr;  // per-launch operators: 3 RK stages, LDG gradient, bare RHS
     std::vector<char> h_const;  // host copy of d_const (for by-value kernel parameters)
     double* d_elem_b = nullptr;  // FP64: cb - ca sigma per element for the 3 RK stages
+    // FP64 with advection: volume fluxes (f_mom, f_mass x, y, z) of the next
+    // stage's input in d_flux[flux_cur], written by the stage that produced
+    // it; flux_valid is false after anything else writes the state.
+    double* d_flux[2] = {nullptr, nullptr};
+    int flux_cur = 0;
+    bool flux_valid = false;
     std::vector<double> h_elem_b;
     double const_dt = 0.0;
     int cur = 0;
