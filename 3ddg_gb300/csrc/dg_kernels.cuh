@@ -156,6 +156,38 @@ struct Pair<double> {
     using type = double2;
 };
 
+// Volume-flux output of the FP64 unpack kernels (f null: none): the fluxes
+// of the state they write, so that the first stage after an upload reads
+// them like any later stage.
+template <typename T>
+struct FluxOut {
+    T* f;
+    T k1, k2, r0;
+    int linear;
+};
+
+// The flux constants of the stage operators and of FluxOut, from one place
+// so that both evaluate bit-identical fluxes.
+template <typename T>
+inline FluxOut<T> flux_consts(T* f, double rho0, double c0, double b_over_a)
+{
+    FluxOut<T> o;
+    o.f = f;
+    o.k1 = (T)(c0 * c0 / rho0);
+    o.k2 = (T)(b_over_a * 0.5 * c0 * c0 / (rho0 * rho0));
+    o.r0 = (T)rho0;
+    o.linear = b_over_a == 0.0 ? 1 : 0;
+    return o;
+}
+
+template <typename T>
+__device__ __forceinline__ void write_fluxes(const FluxOut<T>& fo, size_t fs, size_t o, T d, const T u[3])
+{
+    fo.f[o] = momentum_flux(d, fo.k1, fo.k2);
+#pragma unroll
+    for (int a = 0; a < 3; a++) fo.f[(size_t)(1 + a) * fs + o] = mass_flux(u[a], d, fo.r0, fo.linear);
+}
+
 template <typename T, int K>
 struct GradSmem {
     T r[npt_of(K)];
@@ -921,12 +953,13 @@ inline OpConst<T, K> make_stage_const(double rk_ca, const double* deriv, const d
         C.cQ[a][0] = (T)(0.5 * rk_ca / w[a]);
         C.cQ[a][1] = (T)(-0.5 * rk_ca / w[a]);
     }
-    C.k1 = (T)(c0 * c0 / r0);
-    C.k2 = (T)(b_over_a * 0.5 * c0 * c0 / (r0 * r0));
-    C.r0 = (T)r0;
+    const FluxOut<T> fc = flux_consts<T>(nullptr, r0, c0, b_over_a);
+    C.k1 = fc.k1;
+    C.k2 = fc.k2;
+    C.r0 = fc.r0;
     C.inv_c2 = (T)(1.0 / (c0 * c0));
     C.inv_z = (T)(1.0 / (r0 * c0));
-    C.linear_mass = b_over_a == 0.0 ? 1 : 0;
+    C.linear_mass = fc.linear;
     (void)diff_const;
     return C;
 }
@@ -1015,16 +1048,23 @@ __global__ void pack_host_order_kernel(const T* __restrict__ state, size_t fs, i
 
 template <typename T>
 __global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g,
-                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize)
+                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize,
+                                         FluxOut<T> fo)
 {
     const int Y = g.E[1] * g.K, Z = g.E[2] * g.K, rows = g.E[0] * g.K * Y;
     for (int row = blockIdx.x; row < rows; row += gridDim.x) {
         const RowMap r = row_map(g, row / Y, row % Y);
         for (int kk = threadIdx.x; kk < Z; kk += blockDim.x) {
             const size_t o = row_offset(g, np, r, kk), i = (size_t)row * Z + kk;
-            state[o] = (T)rho[i];
+            const T d = (T)rho[i];
+            T u[3];
+            state[o] = d;
 #pragma unroll
-            for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + o] = (T)vel[a * gsize + i];
+            for (int a = 0; a < 3; a++) {
+                u[a] = (T)vel[a * gsize + i];
+                state[(size_t)(1 + a) * fs + o] = u[a];
+            }
+            if (fo.f) write_fluxes(fo, fs, o, d, u);
         }
     }
 }
@@ -1035,7 +1075,8 @@ __global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int n
 // device memory only; pinned host memory is read by unpack_host_order_kernel.
 template <typename T>
 __global__ void unpack_elem_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g, int n_elem,
-                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize)
+                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize,
+                                         FluxOut<T> fo)
 {
     const int K3 = g.K * g.K * g.K;
     const size_t total = (size_t)n_elem * np;
@@ -1043,9 +1084,15 @@ __global__ void unpack_elem_order_kernel(T* __restrict__ state, size_t fs, int n
         const int e = (int)(s / np), n = (int)(s % np);
         if (n >= K3) continue;
         const size_t i = grid_index(g, e, n);
-        state[s] = (T)rho[i];
+        const T d = (T)rho[i];
+        T u[3];
+        state[s] = d;
 #pragma unroll
-        for (int a = 0; a < 3; a++) state[(size_t)(1 + a) * fs + s] = (T)vel[a * gsize + i];
+        for (int a = 0; a < 3; a++) {
+            u[a] = (T)vel[a * gsize + i];
+            state[(size_t)(1 + a) * fs + s] = u[a];
+        }
+        if (fo.f) write_fluxes(fo, fs, s, d, u);
     }
 }
 

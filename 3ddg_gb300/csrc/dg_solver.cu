@@ -543,25 +543,29 @@ int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_devi
 {
     const GridMap g = grid_map(mesh);
     const int threads = 128, blocks = 152 * 16;
+    // FP64 with advection: the unpack also writes the state's volume fluxes
+    // for the next stage to read.
+    const FluxOut<double> fo = flux_consts<double>(d_flux[flux_cur], p.rho0, p.c0, p.b_over_a);
+    const FluxOut<float> none = flux_consts<float>(nullptr, p.rho0, p.c0, p.b_over_a);
     if (on_device) {
         if (fp64())
             unpack_elem_order_kernel<double><<<blocks, 256, 0, stream>>>((double*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                         g, mesh.n_elem, rho_d, vel_d, gsize());
+                                                                         g, mesh.n_elem, rho_d, vel_d, gsize(), fo);
         else
             unpack_elem_order_kernel<float><<<blocks, 256, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                        g, mesh.n_elem, rho_d, vel_d, gsize());
+                                                                        g, mesh.n_elem, rho_d, vel_d, gsize(), none);
     } else {
         if (fp64())
             unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
-                                                                             mesh.NP, g, rho_d, vel_d, gsize());
+                                                                             mesh.NP, g, rho_d, vel_d, gsize(), fo);
         else
             unpack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((float*)state_ptr(), mesh.fstride(),
-                                                                            mesh.NP, g, rho_d, vel_d, gsize());
+                                                                            mesh.NP, g, rho_d, vel_d, gsize(), none);
     }
     launches++;
     DG_CUDA(cudaGetLastError());
     if (!fp64()) DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
-    flux_valid = false;
+    flux_valid = fp64() && d_flux[0] != nullptr;
     ic_live = false;
     return DG_OK;
 }
