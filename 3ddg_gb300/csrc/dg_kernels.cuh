@@ -41,6 +41,7 @@
 // replaces the halo ring and Grid::communicate.
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 
@@ -320,6 +321,74 @@ __device__ __forceinline__ int line_base(int t)
     return A == 0 ? t : (A == 1 ? (t % K) * K * K + t / K : t * K);
 }
 
+// Even-odd form of one axis's line operator (FP64 line owners).  D is
+// centro-antisymmetric, D[K-1-i][K-1-j] = -D[i][j], and the lift columns are
+// mirrored, L0[K-1-i] = SIG LN[i]; with e_j = v_j + v_{K-1-j},
+// o_j = v_j - v_{K-1-j} (j < H = K/2), s = f0 + fN, d = f0 - fN:
+//   P_i = sum_j E[i][j] e_j + Dc[i] v_H,  Q_i = sum_j O[i][j] o_j,
+//   out_i = P_i + Q_i,  out_{K-1-i} = Q_i - P_i   (i < H; the lift terms
+//   A s, B d are added to P or Q by SIG),
+//   out_H = sum_j Dm[j] o_j + Lm (s or d)   (K odd),
+// E = (D[i][j] + D[i][K-1-j]) / 2, O = (D[i][j] - D[i][K-1-j]) / 2,
+// A = (L0 + LN) / 2, B = (L0 - LN) / 2: at K = 5, 27 FP64 instructions per
+// line and field instead of the 35 of K per-node sums with two lift terms.
+template <int K>
+struct LineEOAxis {
+    static constexpr int H = K / 2;
+    double E[H][H], O[H][H];
+    double Dc[H];          // D[i][H], K odd
+    double Al[H], Bl[H];   // lift combinations
+    double Dm[H];          // D[H][j], K odd
+    double Lm;             // L0[H], K odd
+};
+template <int K>
+struct LineEO {
+    LineEOAxis<K> ax[3];
+};
+
+// One line of one field.  The line owners of a warp cover more than one axis
+// (3 K^2 tasks packed densely), so the axis is a runtime value and its
+// coefficients X come from shared memory: every lane runs the same FP64
+// instructions.
+template <int K, int SIG>
+__device__ __forceinline__ void eo_apply(const LineEOAxis<K>& X, const double v[K], double f0, double fN,
+                                         double out[K])
+{
+    constexpr int H = K / 2;
+    double e[H], o[H];
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+        e[j] = v[j] + v[K - 1 - j];
+        o[j] = v[j] - v[K - 1 - j];
+    }
+    const double s = f0 + fN, d = f0 - fN;
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+        double P = X.E[i][0] * e[0], Q = X.O[i][0] * o[0];
+#pragma unroll
+        for (int j = 1; j < H; j++) {
+            P += X.E[i][j] * e[j];
+            Q += X.O[i][j] * o[j];
+        }
+        if (K & 1) P += X.Dc[i] * v[H];
+        if (SIG > 0) {
+            P += X.Bl[i] * d;
+            Q += X.Al[i] * s;
+        } else {
+            P += X.Al[i] * s;
+            Q += X.Bl[i] * d;
+        }
+        out[i] = P + Q;
+        out[K - 1 - i] = Q - P;
+    }
+    if (K & 1) {
+        double c = X.Lm * (SIG > 0 ? s : d);
+#pragma unroll
+        for (int j = 0; j < H; j++) c += X.Dm[j] * o[j];
+        out[H] = c;
+    }
+}
+
 // Line owner with its own face terms (FP32, K >= 5): the two ends of line t
 // along axis A are the face nodes (A, 0, t) and (A, 1, t), so the owner
 // evaluates both numerical fluxes itself (neighbour values ro/uo/qo[side],
@@ -518,6 +587,64 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
         (void)ia;
     }
+}
+
+// FP64 LDG gradient with even-odd line owners (K where eo_lines<K>()): two
+// elements per CTA so that the 3 K^2 line tasks of each pack densely into
+// warps; each owner loads the neighbour values at its line's two ends, forms
+// the central face sums, and applies the even-odd operator.  One barrier
+// after the element's values reach shared memory, one before the coalesced
+// stores.
+template <int K>
+__host__ __device__ constexpr bool eo_lines()
+{
+    return K == 5;
+}
+
+template <int K>
+__device__ __forceinline__ void grad_eo_line(const LineEOAxis<K>& X, GradSmem<double, K>& S, int a, int t,
+                                             const double ro[2])
+{
+    const int st = axis_stride<K>(a);
+    const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K * K + t / K : t * K);
+    double v[K], out[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+    eo_apply<K, -1>(X, v, ro[0] + v[0], ro[1] + v[K - 1], out);  // flux factors are in the lift columns
+#pragma unroll
+    for (int i = 0; i < K; i++) S.out[a][b0 + i * st] = out[i];
+}
+
+template <int K>
+__global__ void __launch_bounds__(npt_of(K) * 2)
+ldg_gradient_eo_kernel(StageIO<double> io, MeshDev<double> m, const OpConst<double, K>* __restrict__ Cp,
+                       const LineEO<K> L)
+{
+    constexpr int K2 = K * K, K3 = K2 * K, NPT = npt_of(K), EPB = 2, NL = 3 * K2;
+    static_assert(NL <= NPT, "line tasks must fit the element's threads");
+    __shared__ GradSmem<double, K> sm_all[EPB];
+    __shared__ LineEOAxis<K> eo[3];
+    const OpConst<double, K>& C = *Cp;
+    const int n = threadIdx.x;
+    const int e = blockIdx.x * EPB + threadIdx.y;
+    const bool act = n < K3 && e < m.n_elem;
+    if (threadIdx.y == 0 && n < 3) eo[n] = n == 0 ? L.ax[0] : (n == 1 ? L.ax[1] : L.ax[2]);
+    // this thread's line task: element le of the CTA, axis la, line t
+    const int tid = threadIdx.y * NPT + n;
+    const int le = tid / NL, la = (tid % NL) / K2, t = tid % K2;
+    const int el = blockIdx.x * EPB + le;
+    const bool owner = tid < EPB * NL && el < m.n_elem;
+    double rho = 0.0, ro[2] = {0.0, 0.0}, unused_u[2], unused_q[2];
+    if (act) rho = __ldg(io.src + (size_t)e * io.np + n);
+    if (owner) line_end_values<false, false, false, double, K>(io, m, C, el, la, t, ro, unused_u, unused_q);
+    sm_all[threadIdx.y].r[n] = rho;
+    __syncthreads();
+    if (owner) grad_eo_line<K>(eo[la], sm_all[le], la, t, ro);
+    __syncthreads();
+    if (!act) return;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = sm_all[threadIdx.y].out[a][n];
 }
 
 // Shared memory of a stage kernel, per element: for each axis a, the pair
@@ -983,6 +1110,41 @@ inline OpConst<T, K> make_grad_const(const double* deriv, const double* lift0, c
     C.inv_c2 = (T)(1.0 / (c0 * c0));
     C.inv_z = (T)(1.0 / (rho0 * c0));
     return C;
+}
+
+// Even-odd split of the per-axis rows of C (see LineEO); false when D is not
+// centro-antisymmetric or the lift columns are not mirrored with sign SIG, to
+// 1e-12 of their largest entry, and the line owners must not be used.
+template <int K, int SIG>
+inline bool make_line_eo(const OpConst<double, K>& C, LineEO<K>& L)
+{
+    constexpr int H = K / 2;
+    if (H < 1) return false;
+    for (int a = 0; a < 3; a++) {
+        const auto& R = C.rows[a];
+        double dmax = 0.0, lmax = 0.0;
+        for (int i = 0; i < K; i++) {
+            for (int j = 0; j < K; j++) dmax = std::fmax(dmax, std::fabs(R[i][j]));
+            lmax = std::fmax(lmax, std::fmax(std::fabs(R[i][K]), std::fabs(R[i][K + 1])));
+        }
+        for (int i = 0; i < K; i++) {
+            for (int j = 0; j < K; j++)
+                if (std::fabs(R[i][j] + R[K - 1 - i][K - 1 - j]) > 1e-12 * dmax) return false;
+            if (std::fabs(R[K - 1 - i][K] - SIG * R[i][K + 1]) > 1e-12 * lmax) return false;
+        }
+        for (int i = 0; i < H; i++) {
+            for (int j = 0; j < H; j++) {
+                L.ax[a].E[i][j] = 0.5 * (R[i][j] + R[i][K - 1 - j]);
+                L.ax[a].O[i][j] = 0.5 * (R[i][j] - R[i][K - 1 - j]);
+            }
+            L.ax[a].Dc[i] = (K & 1) ? R[i][H] : 0.0;
+            L.ax[a].Al[i] = 0.5 * (R[i][K] + R[i][K + 1]);
+            L.ax[a].Bl[i] = 0.5 * (R[i][K] - R[i][K + 1]);
+            L.ax[a].Dm[i] = (K & 1) ? R[H][i] : 0.0;
+        }
+        L.ax[a].Lm = (K & 1) ? R[H][K] : 0.0;
+    }
+    return true;
 }
 
 // Element-major state  <->  node-duplicated [X][Y][Z] grid layout (the

@@ -139,7 +139,18 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
     dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(1, &ev);
-    ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, const_ptr<T, K>(s, 3), host_const<T, K>(s, 3));
+    bool done = false;
+    if constexpr (!INCR && sizeof(T) == 8 && eo_lines<K>()) {
+        LineEO<K> L;
+        if (make_line_eo<K, -1>(host_const<T, K>(s, 3), L)) {
+            ldg_gradient_eo_kernel<K><<<(md.n_elem + 1) / 2, dim3(npt_of(K), 2), 0, s.stream>>>(
+                io, md, const_ptr<T, K>(s, 3), L);
+            done = true;
+        }
+    }
+    if (!done)
+        ldg_gradient_kernel<T, K, INCR><<<grid, block, 0, s.stream>>>(io, md, const_ptr<T, K>(s, 3),
+                                                                        host_const<T, K>(s, 3));
     s.prof_end(1, ev, grad_bytes(s, io), grad_flops(s));
     s.launches++;
 }
