@@ -671,12 +671,45 @@ struct PlainSmem {
 // since almost every warp holds some node on each face pair.)  The
 // neighbour values of those face nodes are loaded with the thread's own node.
 // ---------------------------------------------------------------------------
+// Elements per CTA of the FP64 stage kernel: two with even-odd line owners
+// (EO), so that the 3 K^2 line tasks of each pack densely into warps.
+template <int K, bool EO>
+__host__ __device__ constexpr int plain_epb()
+{
+    return EO ? 2 : epb_of(K);
+}
+
 // Resident CTAs per SM asked of the compiler for the FP64 stage kernel (0:
-// no request): at K = 5, 64 registers keep 8 CTAs (32 warps) per SM.
-template <typename T, int K>
+// no request): at K = 5, 64 registers keep 32 warps per SM.
+template <typename T, int K, bool EO>
 __host__ __device__ constexpr int plain_min_blocks()
 {
-    return (sizeof(T) == 8 && K == 5) ? 8 : 0;
+    return (sizeof(T) == 8 && K == 5) ? 8 / plain_epb<K, EO>() : 0;
+}
+
+// One line of an FP64 stage kernel with even-odd line owners: the mass
+// equation's line (flux f_mass + G, face terms gr) into S.m and the momentum
+// equation's (f_mom, gm) into S.q, along runtime axis a.
+template <int K>
+__device__ __forceinline__ void stage_eo_line(const LineEOAxis<K>& X, PlainSmem<double, K>& S, int a, int t,
+                                              int do_adv)
+{
+    const int st = axis_stride<K>(a);
+    const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K * K + t / K : t * K);
+    // one field at a time (fewer live registers than both at once)
+    double v[K], out[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st].y;
+    eo_apply<K, 1>(X, v, S.g[a][0][t].y, S.g[a][1][t].y, out);
+#pragma unroll
+    for (int i = 0; i < K; i++) S.m[a][b0 + i * st] = out[i];
+    if (do_adv) {
+#pragma unroll
+        for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st].x;
+        eo_apply<K, 1>(X, v, S.g[a][0][t].x, S.g[a][1][t].x, out);
+#pragma unroll
+        for (int i = 0; i < K; i++) S.q[a][b0 + i * st] = out[i];
+    }
 }
 
 //
@@ -689,22 +722,34 @@ __host__ __device__ constexpr int plain_min_blocks()
 // Mode 2 trades 64 bytes of HBM traffic per node for the FP64 instructions
 // of evaluating every interior face node's neighbour flux a second time
 // (its own element evaluates it for its line sums).
-template <typename T, int K, bool DIFF, int FLUX>
-__global__ void __launch_bounds__(npt_of(K) * epb_of(K), (plain_min_blocks<T, K>()))
-stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, int do_adv, int do_sponge)
+//
+// Line sums (EO): false, every node sums its three lines itself (operator
+// rows in registers); true (D centro-antisymmetric, see LineEO), line owners
+// apply the even-odd operator after the face phase, one more barrier, and
+// each node adds its three axis results.
+template <typename T, int K, bool DIFF, int FLUX, bool EO>
+__global__ void __launch_bounds__(npt_of(K) * plain_epb<K, EO>(), (plain_min_blocks<T, K, EO>()))
+stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, const LineEO<K> L, int do_adv,
+             int do_sponge)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), NF = 6 * K2, R = (NF + NPT - 1) / NPT;
-    __shared__ PlainSmem<T, K> sm_all[epb_of(K)];
+    constexpr int EPB = plain_epb<K, EO>();
+    __shared__ PlainSmem<T, K> sm_all[EPB];
+    __shared__ LineEOAxis<K> eo[EO ? 3 : 1];
     PlainSmem<T, K>& S = sm_all[threadIdx.y];
     const OpConst<T, K>& C = *Cp;
     const int n = threadIdx.x;
-    const int e = blockIdx.x * epb_of(K) + threadIdx.y;
+    const int e = blockIdx.x * EPB + threadIdx.y;
     const bool live = e < m.n_elem;
     const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     const size_t off = (size_t)e * io.np + n;
     OpRows<T, K> R_;
-    R_.load(C, c, act);
+    if constexpr (EO) {
+        if (threadIdx.y == 0 && n < 3) eo[n] = n == 0 ? L.ax[0] : (n == 1 ? L.ax[1] : L.ax[2]);
+    } else {
+        R_.load(C, c, act);
+    }
 
     T rho = T(0), u[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     T fl[4] = {T(0), T(0), T(0), T(0)};
@@ -792,28 +837,44 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
         S.g[F.a][F.side][F.fi].y = gr;
     }
     __syncthreads();
+
+    T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
+    if constexpr (EO) {
+        constexpr int NL = 3 * K2;
+        static_assert(NL <= NPT, "line tasks must fit the element's threads");
+        const int tid = threadIdx.y * NPT + n;
+        const int le = tid / NL, la = (tid % NL) / K2, t = tid % K2;
+        if (tid < EPB * NL && blockIdx.x * EPB + le < m.n_elem) stage_eo_line<K>(eo[la], sm_all[le], la, t, do_adv);
+        __syncthreads();
+        if (!act) return;
+        r_rho = S.m[0][n] + S.m[1][n];
+        r_rho += S.m[2][n];
+#pragma unroll
+        for (int a = 0; a < 3; a++) r_u[a] = do_adv ? S.q[a][n] : T(0);
+    }
     if (!act) return;
 
-    // The density equation is one FMA chain through the three axes (no
-    // per-axis partial sums to add): the kernel is bound by FP64 issue, so
-    // every FP64 instruction saved per node counts.
-    T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
+    if constexpr (!EO) {
+        // The density equation is one FMA chain through the three axes (no
+        // per-axis partial sums to add): the kernel is bound by FP64 issue,
+        // so every FP64 instruction saved per node counts.
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int st = axis_stride<K>(a), base = n - c[a] * st;
-        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
-        T sm = R_.l0[a] * g0.x;
-        sm += R_.ln[a] * gN.x;
-        r_rho += R_.l0[a] * g0.y;
-        r_rho += R_.ln[a] * gN.y;
+        for (int a = 0; a < 3; a++) {
+            const int st = axis_stride<K>(a), base = n - c[a] * st;
+            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+            const typename Pair<T>::type g0 = S.g[a][0][fi], gN = S.g[a][1][fi];
+            T sm = R_.l0[a] * g0.x;
+            sm += R_.ln[a] * gN.x;
+            r_rho += R_.l0[a] * g0.y;
+            r_rho += R_.ln[a] * gN.y;
 #pragma unroll
-        for (int j = 0; j < K; j++) {
-            const typename Pair<T>::type v = S.f[a][base + j * st];
-            sm += R_.d[a][j] * v.x;
-            r_rho += R_.d[a][j] * v.y;
+            for (int j = 0; j < K; j++) {
+                const typename Pair<T>::type v = S.f[a][base + j * st];
+                sm += R_.d[a][j] * v.x;
+                r_rho += R_.d[a][j] * v.y;
+            }
+            r_u[a] = do_adv ? sm : T(0);
         }
-        r_u[a] = do_adv ? sm : T(0);
     }
     // cb - ca sigma of this element: tabulated per stage by the host, so that
     // no thread spends FP64 instructions on it; computed here when absent.

@@ -126,9 +126,11 @@ cudaError_t launch(const dg_params& p, const double* D, const double* L0, const 
     dim3 grid((md.n_elem + dg::epb_of(K) - 1) / dg::epb_of(K));
     if (p.eval_diff) {
         dg::ldg_gradient_kernel<double, K, false><<<grid, block, 0, st>>>(io, md, Gd, G);
-        dg::stage_kernel<double, K, true, 0><<<grid, block, 0, st>>>(io, md, Cd, p.eval_advect, p.eval_sponge);
+        dg::stage_kernel<double, K, true, 0, false><<<grid, block, 0, st>>>(io, md, Cd, dg::LineEO<K>{}, p.eval_advect,
+                                                                          p.eval_sponge);
     } else {
-        dg::stage_kernel<double, K, false, 0><<<grid, block, 0, st>>>(io, md, Cd, p.eval_advect, p.eval_sponge);
+        dg::stage_kernel<double, K, false, 0, false><<<grid, block, 0, st>>>(io, md, Cd, dg::LineEO<K>{}, p.eval_advect,
+                                                                          p.eval_sponge);
     }
     return cudaSuccess;
 }

@@ -156,15 +156,37 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 }
 
 // FP64 stage kernel in the flux mode that io asks for (flux_out: write the
-// output's volume fluxes; flux_in: read the input's).
-template <typename T, int K, bool DIFF>
-void launch_plain(const Solver& s, dim3 grid, dim3 block, const StageIO<T>& io, const MeshDev<T>& md,
-                  const OpConst<T, K>* Cp)
+// output's volume fluxes; flux_in: read the input's), with even-odd line
+// owners where the order has them and the operator allows them.
+template <typename T, int K, bool DIFF, bool EO, int FLUX>
+void launch_plain_eo(const Solver& s, const StageIO<T>& io, const MeshDev<T>& md, const OpConst<T, K>* Cp,
+                     const LineEO<K>& L)
 {
-    const int adv = s.p.eval_advect, sp = s.p.eval_sponge;
-    if (io.flux_out && io.flux_in) stage_kernel<T, K, DIFF, 2><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
-    else if (io.flux_out) stage_kernel<T, K, DIFF, 1><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
-    else stage_kernel<T, K, DIFF, 0><<<grid, block, 0, s.stream>>>(io, md, Cp, adv, sp);
+    const dim3 block(npt_of(K), plain_epb<K, EO>());
+    const dim3 grid((md.n_elem + plain_epb<K, EO>() - 1) / plain_epb<K, EO>());
+    stage_kernel<T, K, DIFF, FLUX, EO><<<grid, block, 0, s.stream>>>(io, md, Cp, L, s.p.eval_advect, s.p.eval_sponge);
+}
+
+template <typename T, int K, bool DIFF, bool EO>
+void launch_plain_mode(const Solver& s, const StageIO<T>& io, const MeshDev<T>& md, const OpConst<T, K>* Cp,
+                       const LineEO<K>& L)
+{
+    if (io.flux_out && io.flux_in) launch_plain_eo<T, K, DIFF, EO, 2>(s, io, md, Cp, L);
+    else if (io.flux_out) launch_plain_eo<T, K, DIFF, EO, 1>(s, io, md, Cp, L);
+    else launch_plain_eo<T, K, DIFF, EO, 0>(s, io, md, Cp, L);
+}
+
+template <typename T, int K, bool DIFF>
+void launch_plain(const Solver& s, int slot, const StageIO<T>& io, const MeshDev<T>& md, const OpConst<T, K>* Cp)
+{
+    LineEO<K> L{};
+    if constexpr (sizeof(T) == 8 && eo_lines<K>()) {
+        if (make_line_eo<K, 1>(host_const<T, K>(s, slot), L)) {
+            launch_plain_mode<T, K, DIFF, true>(s, io, md, Cp, L);
+            return;
+        }
+    }
+    launch_plain_mode<T, K, DIFF, false>(s, io, md, Cp, L);
 }
 
 template <typename T, int K, bool INCR>
@@ -184,8 +206,8 @@ void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slo
             incr_stage_kernel<T, K, false><<<grid, block, 0, s.stream>>>(io, md, Cp, Cv, s.p.eval_advect,
                                                                         s.p.eval_sponge);
     } else {
-        if (s.p.eval_diff) launch_plain<T, K, true>(s, grid, block, io, md, Cp);
-        else launch_plain<T, K, false>(s, grid, block, io, md, Cp);
+        if (s.p.eval_diff) launch_plain<T, K, true>(s, slot, io, md, Cp);
+        else launch_plain<T, K, false>(s, slot, io, md, Cp);
     }
     s.prof_end(0, ev, stage_bytes<T, INCR>(s, io), stage_flops(s, io.old != nullptr || io.inc != nullptr));
     s.launches++;
