@@ -373,16 +373,22 @@ def run_ours(a, dist: Dist):
     traffic = profiled_traffic(kind)
     roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
             "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-            else "fallback 6.8 TB/s", "kernel": "stage_kernel<%s,%d,DIFF>" % (ctype, cfg["ORDER"] + 1),
+            else "fallback 6.8 TB/s",
+            "kernel": ("stage_kernel<double,%d,DIFF,2,EO> (fluxes read, even-odd line owners)" % (cfg["ORDER"] + 1)
+                       if fp64 else "incr_stage_kernel<float,%d,DIFF>" % (cfg["ORDER"] + 1)),
             "algorithmic_bytes_per_launch": st_b / st_n if st_n else None,
             "mean_launch_ms": st_ms / st_n if st_n else None,
             "fp64_pipe": {"achieved_tflops": (st_f / st_n) / (st_ms / st_n / 1e3) / 1e12 if st_n else None,
                           "peak_tflops": FP64_PEAK_TFLOPS,
                           "frac": ((st_f / st_n) / (st_ms / st_n / 1e3) / 1e12) / FP64_PEAK_TFLOPS if st_n else None,
-                          "note": "the FP64 path is bound by the FP64 pipe (1.19 TFLOP/s measured), not HBM"},
+                          "note": "the FP64 path is bound by the FP64 pipe (1.19 TFLOP/s measured), not HBM; "
+                                  "flops counted by the direct formula (K (K + 2) per line), which the even-odd "
+                                  "line owners execute with about 22 % fewer FP64 instructions"},
             "share_of_step": st_ms / ms if ms else None,
-            "ldg_gradient_kernel": {"launches": gr_n, "mean_launch_ms": gr_ms / gr_n if gr_n else None,
-                                    "achieved_gbs": (gr_b / gr_n) / (gr_ms / gr_n / 1e3) / 1e9 if gr_n else None}}
+            "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<%d>" if fp64 else "ldg_gradient_kernel<float,%d>")
+                                        % (cfg["ORDER"] + 1),
+                                "launches": gr_n, "mean_launch_ms": gr_ms / gr_n if gr_n else None,
+                                "achieved_gbs": (gr_b / gr_n) / (gr_ms / gr_n / 1e3) / 1e9 if gr_n else None}}
     line = {
         "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
