@@ -4,7 +4,7 @@ only), multi-step runs to 1e-10 max relative pressure error."""
 import numpy as np
 import pytest
 
-from conftest import max_rel, pressure, workloads
+from conftest import dg, max_rel, pressure, workloads
 
 pytestmark = pytest.mark.gpu
 
@@ -62,17 +62,20 @@ def test_config1_short_matches_oracle(solver_for, oracle_for):
     compare_state(cfg, s, o, STEP_TOL)
 
 
-@pytest.mark.parametrize("periodic", [(1, 0, 0), (0, 1, 1), (1, 1, 1)])
-def test_periodic_matches_oracle(periodic, solver_for, oracle_for):
-    cfg = small(order=3, periodic=periodic)
+# N = 4 runs the FP64 kernels with even-odd line owners, N = 3 with per-node line sums.
+@pytest.mark.parametrize("order,periodic", [(3, (1, 0, 0)), (3, (0, 1, 1)), (3, (1, 1, 1)), (4, (1, 0, 1)),
+                                            (4, (1, 1, 1))])
+def test_periodic_matches_oracle(order, periodic, solver_for, oracle_for):
+    cfg = small(order=order, periodic=periodic)
     s, o = solver_for(cfg), oracle_for(cfg)
     s.step(cfg["DT"], 5)
     o.run(cfg["DT"], 5)
     compare_state(cfg, s, o, STEP_TOL)
 
 
-def test_no_diffusion_no_sponge(solver_for, oracle_for):
-    cfg = small(order=3, diffusion=False)
+@pytest.mark.parametrize("order", [3, 4])
+def test_no_diffusion_no_sponge(order, solver_for, oracle_for):
+    cfg = small(order=order, diffusion=False)
     cfg["EVALUATE_SPONGE"] = 0
     s, o = solver_for(cfg), oracle_for(cfg)
     s.step(cfg["DT"], 5)
@@ -80,8 +83,9 @@ def test_no_diffusion_no_sponge(solver_for, oracle_for):
     compare_state(cfg, s, o, STEP_TOL)
 
 
-def test_linear_mass_flux(solver_for, oracle_for):
-    cfg = small(order=3)
+@pytest.mark.parametrize("order", [3, 4])
+def test_linear_mass_flux(order, solver_for, oracle_for):
+    cfg = small(order=order)
     cfg["B_OVER_A"] = 0.0
     s, o = solver_for(cfg), oracle_for(cfg)
     s.step(cfg["DT"], 5)
@@ -89,10 +93,11 @@ def test_linear_mass_flux(solver_for, oracle_for):
     compare_state(cfg, s, o, STEP_TOL)
 
 
-def test_multiblock_equivalent_to_single_block(solver_for, oracle_for):
+@pytest.mark.parametrize("order", [3, 4])
+def test_multiblock_equivalent_to_single_block(order, solver_for, oracle_for):
     """2x2x2 blocks with the on-device face gather == one block of the same
     global mesh (the reference's MPI exchange makes them identical)."""
-    cfg1 = small(order=3, ne=(6, 4, 6))
+    cfg1 = small(order=order, ne=(6, 4, 6))
     cfg8 = dict(cfg1)
     cfg8["NUM_ELEMENTS"] = [3, 2, 3]
     cfg8["NUM_BLOCKS"] = [2, 2, 2]
@@ -115,10 +120,11 @@ def test_multiblock_equivalent_to_single_block(solver_for, oracle_for):
     compare_state(cfg8, s, o, STEP_TOL)
 
 
-def test_tone_burst_source_matches_oracle(solver_for, oracle_for):
+@pytest.mark.parametrize("order", [3, 4])
+def test_tone_burst_source_matches_oracle(order, solver_for, oracle_for):
     W = workloads()
     cfg = W.scaled(W.config2(seed=0), (6, 6, 8))
-    cfg["ORDER"] = 3
+    cfg["ORDER"] = order
     cfg["SRC_RADIUS"] = 1.2
     cfg["DT"] = W.cfl_dt(cfg)
     s, o = solver_for(cfg), oracle_for(cfg)
@@ -139,6 +145,36 @@ def test_set_state_clears_ic_halo(solver_for, oracle_for):
     s.step(cfg["DT"], 3)
     o.run(cfg["DT"], 3)
     compare_state(cfg, s, o, STEP_TOL)
+
+
+def test_operator_without_mirror_symmetry_matches_oracle(tmp_path):
+    """The N = 4 kernels' even-odd line owners need D to be centro-
+    antisymmetric; a matrix file whose S breaks that (one entry scaled by
+    1 + 1e-6) must take the per-node line sums and still match the oracle
+    running the same operator."""
+    import pyoracle
+    import refinputs
+    refinputs.write_coeff_files(str(tmp_path))
+    with open(tmp_path / "matrices.txt", "w") as f:
+        for N in range(1, refinputs.KMAX):
+            M, S = refinputs.unit_matrices(N, False)
+            S = np.array(S, dtype=np.float64)
+            if N == 4:
+                S[0, 1] *= 1.0 + 1e-6
+            f.write("Order=%d\n" % N)
+            for r in np.asarray(M):
+                f.write(" ".join(refinputs.hexd(v) for v in r) + "\n")
+            for r in S:
+                f.write(" ".join(refinputs.hexd(v) for v in r) + "\n")
+    mf, cf = str(tmp_path / "matrices.txt"), str(tmp_path / "hardcoded_coeff.txt")
+    cfg = small(order=4)
+    M, S = refinputs.read_matrices(mf, 4)
+    assert abs(S[0][1] + S[4][3]) > 1e-8 * abs(S[0][1])  # the mirror symmetry is broken
+    o = pyoracle.Oracle(cfg, M, S, refinputs.read_zeros(cf, 4))
+    with dg().Solver(cfg, mf, cf) as s:
+        s.step(cfg["DT"], 5)
+        o.run(cfg["DT"], 5)
+        compare_state(cfg, s, o, STEP_TOL)
 
 
 @pytest.mark.parametrize("order,kw", [(2, {}), (4, {"periodic": (1, 0, 1)}), (3, {"diffusion": False})])
