@@ -56,7 +56,6 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
     constexpr int R = (NF + NPT - 1) / NPT;
     GradSmem<float, K>* SM = reinterpret_cast<GradSmem<float, K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
-    const int c[3] = {n / K2, (n / K) % K, n % K};
     const float* ub = P.u[P.cur];
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
@@ -151,7 +150,6 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
     constexpr int R = (NF + NPT - 1) / NPT;
     PlainSmem<float, K>* SM = reinterpret_cast<PlainSmem<float, K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
-    const int c[3] = {n / K2, (n / K) % K, n % K};
     const float* ub = P.u[P.cur];
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
     const bool final_stage = stage == 2;

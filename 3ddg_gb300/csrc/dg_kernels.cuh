@@ -531,61 +531,59 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         if (!act) return;
 #pragma unroll
         for (int a2 = 0; a2 < 3; a2++) io.q_out[(size_t)a2 * io.fs + (size_t)e * io.np + n] = S.out[a2][n];
-        return;
-    }
-    // Face nodes assigned densely (see stage_kernel): their neighbour (or
-    // exterior) values are loaded with the thread's own node.
-    int code[R];
+    } else {
+        // Face nodes assigned densely (see stage_kernel): their neighbour (or
+        // exterior) values are loaded with the thread's own node.
+        int code[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = n + r * NPT;
-        code[r] = 0;
-        if (live && t < NF) {
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            code[r] = 0;
+            if (live && t < NF) {
+                const FaceNode<K> F(t);
+                code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+            }
+        }
+        T rho = T(0);
+        if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
+        T ro[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            ro[r] = T(0);
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
             const FaceNode<K> F(t);
-            code[r] = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+            if (code[r] >= 0) {
+                ro[r] = load_in<INCR>(io, 0, (size_t)code[r] * io.np + F.nn);
+            } else {
+                T uo;
+                exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo);
+            }
         }
-    }
-    T rho = T(0);
-    if (act) rho = load_in<INCR>(io, 0, (size_t)e * io.np + n);
-    T ro[R];
+        OpRows<T, K> R_;
+        R_.load(C, c, act);
+        S.r[n] = rho;
+        __syncthreads();
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        ro[r] = T(0);
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        if (code[r] >= 0) {
-            ro[r] = load_in<INCR>(io, 0, (size_t)code[r] * io.np + F.nn);
-        } else {
-            T uo;
-            exterior<T, K>(m, C, -1 - code[r], F.side, F.fi, ro[r], uo);
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            S.fl[F.a][F.side][F.fi] = ro[r] + S.r[F.nf];  // flux factors are in the lift columns
         }
-    }
-    OpRows<T, K> R_;
-    if constexpr (!LINES) R_.load(C, c, act);
-    S.r[n] = rho;
-    __syncthreads();
+        __syncthreads();
+        if (!act) return;
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        S.fl[F.a][F.side][F.fi] = ro[r] + S.r[F.nf];  // flux factors are in the lift columns
-    }
-    __syncthreads();
-    if (!act) return;
+        for (int a = 0; a < 3; a++) {
+            const int st = axis_stride<K>(a);
+            const int base = n - c[a] * st;
+            const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
+            T s = R_.l0[a] * S.fl[a][0][fi];
+            s += R_.ln[a] * S.fl[a][1][fi];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int st = axis_stride<K>(a);
-        const int ia = c[a];
-        const int base = n - ia * st;
-        const int fi = c[(a + 1) % 3] * K + c[(a + 2) % 3];
-        T s = R_.l0[a] * S.fl[a][0][fi];
-        s += R_.ln[a] * S.fl[a][1][fi];
-#pragma unroll
-        for (int j = 0; j < K; j++) s += R_.d[a][j] * S.r[base + j * st];
-        io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
-        (void)ia;
+            for (int j = 0; j < K; j++) s += R_.d[a][j] * S.r[base + j * st];
+            io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = s;
+        }
     }
 }
 
