@@ -90,11 +90,11 @@ int Batch::init(int device_capacity)
     cudaDeviceProp prop;
     DGB_CUDA(cudaGetDeviceProperties(&prop, device));
     num_sms = prop.multiProcessorCount;
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2], batch_stage_kernel<2>, BATCH_THREADS, 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3], batch_stage_kernel<3>, BATCH_THREADS, 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4], batch_stage_kernel<4>, BATCH_THREADS, 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5], batch_stage_kernel<5>, BATCH_THREADS, 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6], batch_stage_kernel<6>, BATCH_THREADS, 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2], batch_stage_kernel<2>, bthreads_of(2), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3], batch_stage_kernel<3>, bthreads_of(3), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4], batch_stage_kernel<4>, bthreads_of(4), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5], batch_stage_kernel<5>, bthreads_of(5), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6], batch_stage_kernel<6>, bthreads_of(6), 0));
     max_ctas_per_sm = 1;
     for (int k = 2; k <= BATCH_KMAX; k++) {
         occ_k[k] = std::max(1, occ_k[k]);
@@ -342,11 +342,11 @@ int Batch::launch_step()
             const int grid = std::max(1, std::min(num_sms * std::min(ctas_per_sm, occ_k[K]), A.n_tiles));
             for (int phase = 0; phase < 2; phase++) {
                 switch (K) {
-                case 2: batch_stage_kernel<2><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
-                case 3: batch_stage_kernel<3><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
-                case 4: batch_stage_kernel<4><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
-                case 5: batch_stage_kernel<5><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
-                case 6: batch_stage_kernel<6><<<grid, BATCH_THREADS, 0, bs>>>(A, grp.ops, phase); break;
+                case 2: batch_stage_kernel<2><<<grid, bthreads_of(2), 0, bs>>>(A, grp.ops, phase); break;
+                case 3: batch_stage_kernel<3><<<grid, bthreads_of(3), 0, bs>>>(A, grp.ops, phase); break;
+                case 4: batch_stage_kernel<4><<<grid, bthreads_of(4), 0, bs>>>(A, grp.ops, phase); break;
+                case 5: batch_stage_kernel<5><<<grid, bthreads_of(5), 0, bs>>>(A, grp.ops, phase); break;
+                case 6: batch_stage_kernel<6><<<grid, bthreads_of(6), 0, bs>>>(A, grp.ops, phase); break;
                 }
                 DGB_CUDA(cudaGetLastError());
                 launches++;

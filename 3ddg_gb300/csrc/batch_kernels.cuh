@@ -10,7 +10,7 @@
 // (batch_stage_kernel<K>, K = N + 1 <= 6) that pull tiles (problem, first
 // element, element count) from an atomic counter: the LDG gradient of every
 // tile, then the stage update of every tile, with EPB(K) elements per pass of
-// a 256-thread CTA; the number of passes per tile (tile size) is chosen per
+// a CTA of bthreads_of(K) threads; the number of passes per tile (tile size) is chosen per
 // order by the autotuner.  Groups run as parallel branches of the step.  The
 // arithmetic per element is the one of incr_stage_kernel /
 // ldg_gradient_kernel (dg_kernels.cuh) with 1/w_a applied after the line
@@ -26,7 +26,11 @@
 
 namespace dg {
 
-__host__ __device__ constexpr int bepb_of(int K) { return BATCH_THREADS / npt_of(K); }
+// Threads per CTA of order K: 256, except one element's 224 node slots at
+// K = 6, where a 256-thread CTA would carry an idle warp that holds registers
+// (and resident-CTA slots) without work in the node phases.
+__host__ __device__ constexpr int bthreads_of(int K) { return K == 6 ? npt_of(6) : BATCH_THREADS; }
+__host__ __device__ constexpr int bepb_of(int K) { return bthreads_of(K) / npt_of(K); }
 
 __device__ __forceinline__ void batch_exterior(const BatchProblem& P, int face, int stage, float& ro, float& uo)
 {
@@ -314,9 +318,11 @@ __host__ __device__ constexpr size_t batch_smem_bytes()
 }
 
 // Resident CTAs per SM asked of the compiler for order K (register budget
-// 65536 / (256 x blocks)), chosen by measurement on config 4: 5 (48
-// registers) for K = 2, 4, 6 (no spills at K = 2, 4; 20 bytes at K = 6), 4 (64
-// registers) for K = 3, 5, which spill heavily at 48.
+// 65536 / (threads x blocks)), chosen by measurement on config 4: 5 (48
+// registers) for K = 2, 4 (no spills), 4 (64 registers) for K = 3, 5, which
+// spill heavily at 48, and 5 CTAs of 224 threads (56 registers, no spills)
+// for K = 6: 123.3 G, against 121.9 G with 6 CTAs at 48 registers and
+// 121.5 G with 256-thread CTAs.
 __host__ __device__ constexpr int batch_min_blocks(int K)
 {
     return K == 2 || K == 4 || K == 6 ? 5 : 4;
@@ -336,7 +342,7 @@ __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProbl
 // step without any kernel waiting on another's blocks.  A persistent grid
 // pulls the group's tiles from an atomic counter.
 template <int K>
-__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(K))
+__global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K))
     batch_stage_kernel(BatchArgs A, const BatchOps ops, int phase)
 {
     __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
