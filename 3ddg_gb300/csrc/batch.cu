@@ -90,15 +90,22 @@ int Batch::init(int device_capacity)
     cudaDeviceProp prop;
     DGB_CUDA(cudaGetDeviceProperties(&prop, device));
     num_sms = prop.multiProcessorCount;
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2], batch_stage_kernel<2>, bthreads_of(2), 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3], batch_stage_kernel<3>, bthreads_of(3), 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4], batch_stage_kernel<4>, bthreads_of(4), 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5], batch_stage_kernel<5>, bthreads_of(5), 0));
-    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6], batch_stage_kernel<6>, bthreads_of(6), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2][0], batch_stage_kernel<2, 0>, bthreads_of(2), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[2][1], batch_stage_kernel<2, 1>, bthreads_of(2), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3][0], batch_stage_kernel<3, 0>, bthreads_of(3), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[3][1], batch_stage_kernel<3, 1>, bthreads_of(3), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4][0], batch_stage_kernel<4, 0>, bthreads_of(4), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[4][1], batch_stage_kernel<4, 1>, bthreads_of(4), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5][0], batch_stage_kernel<5, 0>, bthreads_of(5), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[5][1], batch_stage_kernel<5, 1>, bthreads_of(5), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6][0], batch_stage_kernel<6, 0>, bthreads_of(6), 0));
+    DGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_k[6][1], batch_stage_kernel<6, 1>, bthreads_of(6), 0));
     max_ctas_per_sm = 1;
     for (int k = 2; k <= BATCH_KMAX; k++) {
-        occ_k[k] = std::max(1, occ_k[k]);
-        max_ctas_per_sm = std::max(max_ctas_per_sm, occ_k[k]);
+        for (int ph = 0; ph < 2; ph++) {
+            occ_k[k][ph] = std::max(1, occ_k[k][ph]);
+            max_ctas_per_sm = std::max(max_ctas_per_sm, occ_k[k][ph]);
+        }
     }
     ctas_per_sm = max_ctas_per_sm;
     capacity = std::max(1, device_capacity);
@@ -339,14 +346,20 @@ int Batch::launch_step()
             A.stage = s;
             // persistent grid, but no more CTAs than the group has tiles: a small
             // group (few problems in flight) leaves room for the other branches
-            const int grid = std::max(1, std::min(num_sms * std::min(ctas_per_sm, occ_k[K]), A.n_tiles));
             for (int phase = 0; phase < 2; phase++) {
-                switch (K) {
-                case 2: batch_stage_kernel<2><<<grid, bthreads_of(2), 0, bs>>>(A, grp.ops, phase); break;
-                case 3: batch_stage_kernel<3><<<grid, bthreads_of(3), 0, bs>>>(A, grp.ops, phase); break;
-                case 4: batch_stage_kernel<4><<<grid, bthreads_of(4), 0, bs>>>(A, grp.ops, phase); break;
-                case 5: batch_stage_kernel<5><<<grid, bthreads_of(5), 0, bs>>>(A, grp.ops, phase); break;
-                case 6: batch_stage_kernel<6><<<grid, bthreads_of(6), 0, bs>>>(A, grp.ops, phase); break;
+                const int grid =
+                    std::max(1, std::min(num_sms * std::min(ctas_per_sm, occ_k[K][phase]), A.n_tiles));
+                switch (K * 2 + phase) {
+                case 4: batch_stage_kernel<2, 0><<<grid, bthreads_of(2), 0, bs>>>(A, grp.ops); break;
+                case 5: batch_stage_kernel<2, 1><<<grid, bthreads_of(2), 0, bs>>>(A, grp.ops); break;
+                case 6: batch_stage_kernel<3, 0><<<grid, bthreads_of(3), 0, bs>>>(A, grp.ops); break;
+                case 7: batch_stage_kernel<3, 1><<<grid, bthreads_of(3), 0, bs>>>(A, grp.ops); break;
+                case 8: batch_stage_kernel<4, 0><<<grid, bthreads_of(4), 0, bs>>>(A, grp.ops); break;
+                case 9: batch_stage_kernel<4, 1><<<grid, bthreads_of(4), 0, bs>>>(A, grp.ops); break;
+                case 10: batch_stage_kernel<5, 0><<<grid, bthreads_of(5), 0, bs>>>(A, grp.ops); break;
+                case 11: batch_stage_kernel<5, 1><<<grid, bthreads_of(5), 0, bs>>>(A, grp.ops); break;
+                case 12: batch_stage_kernel<6, 0><<<grid, bthreads_of(6), 0, bs>>>(A, grp.ops); break;
+                case 13: batch_stage_kernel<6, 1><<<grid, bthreads_of(6), 0, bs>>>(A, grp.ops); break;
                 }
                 DGB_CUDA(cudaGetLastError());
                 launches++;

@@ -44,7 +44,7 @@ struct Batch {
     cudaStream_t branch[kBranches] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[kBranches] = {};
     int num_sms = 0, max_ctas_per_sm = 1, ctas_per_sm = 1;
-    int occ_k[BATCH_KMAX + 1] = {};          // resident CTAs per SM of each order's kernel
+    int occ_k[BATCH_KMAX + 1][2] = {};       // resident CTAs per SM of each order's kernel, per phase
     // Problems of one order sharing one operator (order, mass matrix, basis
     // files) form a group: one kernel launch per group and stage.
     struct Group {

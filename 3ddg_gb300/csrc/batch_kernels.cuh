@@ -317,15 +317,21 @@ __host__ __device__ constexpr size_t batch_smem_bytes()
     return bepb_of(K) * sizeof(PlainSmem<float, K>);
 }
 
-// Resident CTAs per SM asked of the compiler for order K (register budget
+// Resident CTAs per SM asked of the compiler for the gradient phase (register
+// budget 65536 / (256 x 8) = 32; spills of 8-36 bytes at some orders): 136.3 G
+// on config 4, against 131.1 G at 6 (42 registers) and 123.3 G with both
+// phases in one kernel at the stage phase's budget.
+constexpr int BATCH_GRAD_BLOCKS = 8;
+
+// Resident CTAs per SM asked of the compiler for order K's stage phase (register
 // 65536 / (threads x blocks)), chosen by measurement on config 4: 5 (48
 // registers) for K = 2, 4 (no spills), 4 (64 registers) for K = 3, 5, which
 // spill heavily at 48, and 5 CTAs of 224 threads (56 registers, no spills)
 // for K = 6: 123.3 G, against 121.9 G with 6 CTAs at 48 registers and
 // 121.5 G with 256-thread CTAs.
-__host__ __device__ constexpr int batch_min_blocks(int K)
+__host__ __device__ constexpr int batch_min_blocks(int K, int phase)
 {
-    return K == 2 || K == 4 || K == 6 ? 5 : 4;
+    return phase == 0 ? BATCH_GRAD_BLOCKS : (K == 2 || K == 4 || K == 6 ? 5 : 4);
 }
 
 __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProblem* src)
@@ -336,20 +342,21 @@ __device__ __forceinline__ void load_problem(BatchProblem& dst, const BatchProbl
 }
 
 // One phase of one RK stage of every active problem of a group of order K:
-// phase 0 the LDG gradient of every tile, phase 1 the stage update of every
+// PHASE 0 the LDG gradient of every tile, PHASE 1 the stage update of every
 // tile.  The two phases are separate launches (the kernel boundary is the
 // barrier between them), so that groups can run as parallel branches of the
-// step without any kernel waiting on another's blocks.  A persistent grid
-// pulls the group's tiles from an atomic counter.
-template <int K>
-__global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K))
-    batch_stage_kernel(BatchArgs A, const BatchOps ops, int phase)
+// step without any kernel waiting on another's blocks, and separate kernels,
+// so that each gets its own register budget.  A persistent grid pulls the
+// group's tiles from an atomic counter.
+template <int K, int PHASE>
+__global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K, PHASE))
+    batch_stage_kernel(BatchArgs A, const BatchOps ops)
 {
     __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
     __shared__ BatchProblem P;
     __shared__ int tile_idx;
     for (;;) {
-        if (threadIdx.x == 0) tile_idx = atomicAdd(A.counters + phase, 1);
+        if (threadIdx.x == 0) tile_idx = atomicAdd(A.counters + PHASE, 1);
         __syncthreads();
         const int ti = tile_idx;
         if (ti >= A.n_tiles) break;
@@ -357,7 +364,7 @@ __global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K))
         load_problem(P, A.probs + T.prob);
         __syncthreads();
         if (P.active) {
-            if (phase == 0) batch_grad_tile<K>(P, ops, T, A.stage, smraw);
+            if constexpr (PHASE == 0) batch_grad_tile<K>(P, ops, T, A.stage, smraw);
             else batch_stage_tile<K>(P, ops, T, A.stage, smraw);
         }
         __syncthreads();
