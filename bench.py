@@ -43,7 +43,8 @@ def args_():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="RK steps of the end-to-end run (0: the same --steps as the device-timed run)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-extras", action="store_true", help="skip the FP32 form and error runs")
     ap.add_argument("--elements", type=int, default=0,
@@ -322,7 +323,7 @@ def run_ours(a, dist: Dist):
     vel_o = torch.empty((3, X, Y, Z), dtype=torch.float64, pin_memory=True)
     rho, vel, rho_out, vel_out = rho_t.numpy(), vel_t.numpy(), rho_o.numpy(), vel_o.numpy()
     s.state(rho, vel)
-    ne2e = max(1, a.e2e_steps)
+    ne2e = max(1, a.e2e_steps if a.e2e_steps > 0 else a.steps)
     dist.barrier()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
