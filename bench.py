@@ -487,8 +487,25 @@ def batched_form(a, dg, W, torch):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         launches = b.launches - l0
+        # error of the FP32 batch against the FP64 plain path, one problem per order
+        err = {}
+        picks = {}
+        for i, c in enumerate(cfgs):
+            picks.setdefault(c["ORDER"], i)
+        for order, i in sorted(picks.items()):
+            _, done, _ = b.info(i)
+            r32, _ = b.state(i)
+            c64 = dict(cfgs[i], PRECISION=64)
+            with dg.Solver(c64) as s64:
+                s64.step(c64["DT"], int(done))
+                r64, _ = s64.state()
+            p32, p64 = pressure(c64, r32), pressure(c64, r64)
+            err["N=%d" % order] = {"problem": i, "steps": int(done),
+                                   "l2_rel_pressure": float(np.linalg.norm(p32 - p64) / np.linalg.norm(p64)),
+                                   "linf_rel_pressure": float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)))}
     return {"value": 4 * nodes * 3 * steps / (ms / 1e3), "unit": UNIT, "problems": len(cfgs), "nodes": nodes,
             "orders": sorted({c["ORDER"] for c in cfgs}), "steps": steps, "ms_per_step": ms / steps,
+            "error_vs_fp64": err,
             "autotune": tune, "autotune_s": tune_s, "graph_launches_per_step": launches / steps,
             "workload": "config4: %d instances, elements 4..24 per axis, N 2..5, FP32 Kahan, tone burst, sponge"
                         % len(cfgs)}
@@ -547,6 +564,27 @@ def serving_form(a, dg, W):
             row["fp64_one_at_a_time"] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                                          "solves_per_s": len(lat) / span, "dof_stage_updates_per_s": work / span}
         out["rates"].append(row)
+    # error of served results against the FP64 plain path: one request per order of the first
+    # trace, served together (untimed, results kept) and each solved alone in FP64
+    cfgs, _ = serving_trace(a.serve_rates[0], a.serve_requests, 40, W)
+    picks = {}
+    for c in cfgs:
+        picks.setdefault(c["ORDER"], c)
+    err = {}
+    with dg.Server(150 << 30, keep_results=True) as srv:
+        rids = {order: srv.submit(c) for order, c in sorted(picks.items())}
+        srv.run(max_seconds=600)
+        for order, rid in rids.items():
+            c64 = dict(picks[order], PRECISION=64)
+            r32 = srv.result(rid, state=True)["rho"]
+            with dg.Solver(c64) as s64:
+                s64.step(c64["DT"], c64["STEPS"])
+                r64, _ = s64.state()
+            p32, p64 = pressure(c64, r32), pressure(c64, r64)
+            err["N=%d" % order] = {"steps": c64["STEPS"],
+                                   "l2_rel_pressure": float(np.linalg.norm(p32 - p64) / np.linalg.norm(p64)),
+                                   "linf_rel_pressure": float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)))}
+    out["error_vs_fp64"] = err
     return out
 
 
