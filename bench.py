@@ -173,6 +173,20 @@ def measured_peaks():
 
 FP64_PEAK_TFLOPS = 1.19  # FP64 FMA throughput measured on a GB300 (profiles/fp64_fp32_peak_probe.md)
 
+# Algorithmic HBM bytes per DOF-stage-update of the FP32 increment form with diffusion (4 DOFs per
+# node): stage kernel (11 + 15 + 23) / 3 values of 4 B per node over the three stages (input u, d,
+# G, compensation in; d or u', compensation out), gradient kernel (4 + 5 + 5) / 3 values; 84 B per
+# node-stage.
+FP32_BYTES_PER_DOF_STAGE = 84.0 / 4
+
+
+def hbm_roofline(value):
+    """Whole-job HBM fraction of an FP32 form's throughput from its algorithmic bytes."""
+    peak, kind = measured_peaks()
+    gbs = value * FP32_BYTES_PER_DOF_STAGE / 1e9
+    return {"bound": "hbm", "algorithmic_bytes_per_dof_stage": FP32_BYTES_PER_DOF_STAGE, "achieved_gbs": gbs,
+            "peak_gbs": peak, "frac": gbs / peak, "peak_source": kind}
+
 
 def profiled_traffic(kind: str):
     """Per-launch DRAM traffic of the dominant kernel from the committed ncu
@@ -505,7 +519,7 @@ def batched_form(a, dg, W, torch):
                                    "linf_rel_pressure": float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)))}
     return {"value": 4 * nodes * 3 * steps / (ms / 1e3), "unit": UNIT, "problems": len(cfgs), "nodes": nodes,
             "orders": sorted({c["ORDER"] for c in cfgs}), "steps": steps, "ms_per_step": ms / steps,
-            "error_vs_fp64": err,
+            "error_vs_fp64": err, "roofline": hbm_roofline(4 * nodes * 3 * steps / (ms / 1e3)),
             "autotune": tune, "autotune_s": tune_s, "graph_launches_per_step": launches / steps,
             "workload": "config4: %d instances, elements 4..24 per axis, N 2..5, FP32 Kahan, tone burst, sponge"
                         % len(cfgs)}
@@ -544,6 +558,7 @@ def serving_form(a, dg, W):
                "dof_stage_updates": work,
                # served throughput over the trace's span (first arrival to last completion)
                "dof_stage_updates_per_s": work * st["solves_per_s"] / max(1, st["completed"])}
+        row["hbm_frac"] = hbm_roofline(row["dof_stage_updates_per_s"])["frac"]
         if rate in a.serve_baseline_rates:
             lat, span0, span1, prev_done = [], None, 0.0, 0.0
             start = time.perf_counter()
