@@ -26,10 +26,14 @@
 // the equations' lift scales go into per-axis copies of D and into the
 // face-flux coefficients, the gradient carries -D_c so that the LDG
 // divergence and the mass-flux divergence share one line sum, and the sponge
-// folds into the RK combination.  Per node and stage each axis costs
-// 2 (K + 2) FMAs for the volume and lift terms; the element's face nodes are
-// dealt out densely to its threads so that no warp issues face arithmetic for
-// lanes that have none.
+// folds into the RK combination (its per-element weight tabulated by the
+// host).  The element's face nodes are dealt out densely to its threads so
+// that no warp issues face arithmetic for lanes that have none; each stage
+// writes the volume fluxes of its output for the next stage to read (flux
+// modes), so no face neighbour's flux is evaluated twice; and at K = 5 the
+// line sums use the even-odd split of the centro-antisymmetric D (LineEO),
+// with line owners packed densely two elements per CTA, instead of per-node
+// sums of 2 (K + 2) FMAs per axis.
 //
 // FP32 (bound by the L1 data pipe, load latency and issue): for K >= 5 line
 // owners (a warp per axis, a lane per line) evaluate their line's two face
