@@ -9,7 +9,7 @@ namespace dg {
 
 std::string validate_params(const dg_params& p)
 {
-    if (p.order < 1 || p.order > 8) return "ORDER must be in 1..8";
+    if (p.order < 1 || p.order > 7) return "ORDER must be in 1..7";  // kernels for K = 2..8 nodes per line
     for (int a = 0; a < 3; a++) {
         if (p.num_blocks[a] < 1) return "NUM_BLOCKS must be >= 1";
         if (p.num_elements[a] < 1) return "NUM_ELEMENTS must be >= 1";

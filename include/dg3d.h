@@ -35,7 +35,7 @@ extern "C" {
  * the Grid constructor arguments (cppsrc/Grid.h:33) and struct BCParam
  * (cppsrc/BCParam.h:13-36). */
 typedef struct dg_params {
-    int order;                 /* ORDER: polynomial order N (nodes per line N+1), 1..8 */
+    int order;                 /* ORDER: polynomial order N (nodes per line N+1), 1..7 */
     int num_blocks[3];         /* NUM_BLOCKS */
     int num_elements[3];       /* NUM_ELEMENTS, per block */
     double elem_width[3];      /* ELEMENT_WIDTH */

@@ -8,7 +8,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, dg
+from conftest import ROOT, dg, workloads
 
 HEADER = os.path.join(ROOT, "include", "dg3d.h")
 
@@ -167,6 +167,17 @@ def test_order_out_of_range_rejected():
     m = dg()
     with pytest.raises(m.DGError):
         m.line_operators(0)
+
+
+@pytest.mark.parametrize("order", [0, 8])
+def test_solver_order_outside_kernels_rejected_at_create(order):
+    """The kernels cover 2..8 nodes per line: other orders fail in dg_create,
+    before any device work, not at the first step."""
+    m = dg()
+    cfg = workloads().gaussian_pulse(num_elements=(2, 2, 2), order=3)
+    cfg["ORDER"] = order
+    with pytest.raises(m.DGError, match="ORDER must be in 1..7"):
+        m.Solver(cfg)
 
 
 def test_hdf5_roundtrip(tmp_path):
