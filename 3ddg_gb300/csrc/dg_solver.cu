@@ -193,11 +193,11 @@ template <typename T, int K, bool INCR>
 void launch_stage(Solver& s, const StageIO<T>& io, const MeshDev<T>& md, int slot)
 {
     const OpConst<T, K>* Cp = const_ptr<T, K>(s, slot);
-    dim3 block(npt_of(K), epb_of(K));
-    dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
     cudaEvent_t ev = nullptr;
     s.prof_begin(0, &ev);
     if constexpr (INCR) {
+        const dim3 block(npt_of(K), epb_of(K));
+        const dim3 grid((md.n_elem + epb_of(K) - 1) / epb_of(K));
         const OpConst<T, K>& Cv = host_const<T, K>(s, slot);
         if (s.p.eval_diff)
             incr_stage_kernel<T, K, true><<<grid, block, 0, s.stream>>>(io, md, Cp, Cv, s.p.eval_advect,
