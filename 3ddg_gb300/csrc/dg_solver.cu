@@ -1044,6 +1044,9 @@ int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double
 int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem)
 {
     if (!h || !base) return fail(DG_ERR_INVALID, "dg_state_device: null argument");
+    // the caller may write the state: the next FP64 stage evaluates the volume
+    // fluxes from it instead of reading the ones cached by the last stage
+    h->s.flux_valid = false;
     const size_t es = h->s.fp64() ? 8 : 4;
     char* b = (char*)h->s.state_ptr();
     for (int f = 0; f < 4; f++) base[f] = b + (size_t)f * h->s.mesh.fstride() * es;

@@ -247,7 +247,11 @@ int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double
 
 /* Device pointers of the current state fields (FP64 or FP32 per precision),
  * element-major: field f, element e, node n at base[f] + e*node_stride + n,
- * node n = (i*K + j)*K + k.  For zero-copy integration and benchmarking. */
+ * node n = (i*K + j)*K + k.  For zero-copy integration and benchmarking.
+ * Writes through them must be ordered against the library's stream
+ * (dg_stream) and made before the next dg_step; to write again after later
+ * steps, call dg_state_device again first (the FP64 path caches the volume
+ * fluxes of the state between stages, and this call drops that cache). */
 int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem);
 
 /* ------------------------------------------------------------------------

@@ -199,6 +199,36 @@ def test_flux_buffers_bitwise_after_state_round_trip(order, kw, solver_for):
     assert np.array_equal(ra, rb) and np.array_equal(va, vb)
 
 
+def test_state_written_in_device_memory_is_seen_by_the_next_step(solver_for):
+    """dg_state_device hands out the state for zero-copy coupling: a state
+    written through it (here halved in place by torch) must be stepped from
+    its own volume fluxes, not the ones cached for the old state, exactly as
+    the same state set through dg_set_state."""
+    import torch
+
+    class DeviceArray:
+        def __init__(self, ptr, n):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 2}
+
+    cfg = small(order=4)
+    a, b = solver_for(cfg), solver_for(cfg)
+    a.step(cfg["DT"], 2)
+    b.step(cfg["DT"], 2)
+    base, NP, n_elem = a.device_state()
+    a.synchronize()
+    for f in range(4):
+        torch.as_tensor(DeviceArray(base[f], n_elem * NP), device="cuda").mul_(0.5)
+    torch.cuda.synchronize()
+    r, v = b.state()
+    b.set_state(0.5 * r, 0.5 * v)
+    a.step(cfg["DT"], 2)
+    b.step(cfg["DT"], 2)
+    ra, va = a.state()
+    rb, vb = b.state()
+    assert np.max(np.abs(ra)) > 0
+    assert np.array_equal(ra, rb) and np.array_equal(va, vb)
+
+
 @pytest.mark.parametrize("precision", [64, 32])
 def test_pinned_host_buffers_match_pageable(precision, solver_for):
     """Pinned host buffers are read/written by the kernels directly; pageable
