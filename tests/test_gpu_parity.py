@@ -84,6 +84,26 @@ def test_no_diffusion_no_sponge(order, solver_for, oracle_for):
 
 
 @pytest.mark.parametrize("order", [3, 4])
+def test_diffusion_only(order, solver_for, oracle_for):
+    """EVALUATE_ADVECTION = 0: no volume fluxes (no flux buffers), the line
+    owners skip the momentum lines; FP32 against FP64 as well."""
+    cfg = small(order=order)
+    cfg["EVALUATE_ADVECTION"] = 0
+    cfg["DIFF_CONST"] = 0.05
+    s, o = solver_for(cfg), oracle_for(cfg)
+    s.step(cfg["DT"], 5)
+    o.run(cfg["DT"], 5)
+    compare_state(cfg, s, o, STEP_TOL)
+    r0, _ = o.state()
+    assert np.max(np.abs(r0)) > 0
+    s32 = solver_for(dict(cfg, PRECISION=32))
+    s32.step(cfg["DT"], 5)
+    r64, _ = s.state()
+    r32, _ = s32.state()
+    assert np.linalg.norm(r32 - r64) <= 1e-5 * np.linalg.norm(r64)
+
+
+@pytest.mark.parametrize("order", [3, 4])
 def test_linear_mass_flux(order, solver_for, oracle_for):
     cfg = small(order=order)
     cfg["B_OVER_A"] = 0.0
