@@ -392,6 +392,9 @@ def run_ours(a, dist: Dist):
             "kernel": ("stage_kernel<double,%d,DIFF,2,EO> (fluxes read, even-odd line owners)" % (cfg["ORDER"] + 1)
                        if fp64 else "incr_stage_kernel<float,%d,DIFF>" % (cfg["ORDER"] + 1)),
             "algorithmic_bytes_per_launch": st_b / st_n if st_n else None,
+            "traffic_note": ("above the algorithmic bytes by the volume-flux buffers (4 values written and 4 read "
+                             "per node, 64 B): HBM traded for the FP64 work of evaluating each face neighbour's "
+                             "flux a second time" if fp64 else None),
             "mean_launch_ms": st_ms / st_n if st_n else None,
             "fp64_pipe": {"achieved_tflops": (st_f / st_n) / (st_ms / st_n / 1e3) / 1e12 if st_n else None,
                           "peak_tflops": FP64_PEAK_TFLOPS,
