@@ -182,6 +182,11 @@ def test_anisotropic_elements_match_oracle(order, solver_for, oracle_for):
     s.step(cfg["DT"], 5)
     o.run(cfg["DT"], 5)
     compare_state(cfg, s, o, STEP_TOL)
+    s32 = solver_for(dict(cfg, PRECISION=32))
+    s32.step(cfg["DT"], 5)
+    r64, _ = s.state()
+    r32, _ = s32.state()
+    assert np.linalg.norm(r32 - r64) <= 1e-5 * np.linalg.norm(r64)
 
 
 @pytest.mark.parametrize("order", [3, 4])
