@@ -328,7 +328,9 @@ constexpr int BATCH_GRAD_BLOCKS = 8;
 // registers) for K = 2, 4 (no spills), 4 (64 registers) for K = 3, 5, which
 // spill heavily at 48, and 5 CTAs of 224 threads (56 registers, no spills)
 // for K = 6: 123.3 G, against 121.9 G with 6 CTAs at 48 registers and
-// 121.5 G with 256-thread CTAs.
+// 121.5 G with 256-thread CTAs (with both phases in one kernel); with the
+// phases apart, the K = 6 update at 48 registers (6 CTAs, 4 bytes of spills)
+// measured 134.8 against 135.2 G.
 __host__ __device__ constexpr int batch_min_blocks(int K, int phase)
 {
     return phase == 0 ? BATCH_GRAD_BLOCKS : (K == 2 || K == 4 || K == 6 ? 5 : 4);
