@@ -3,7 +3,8 @@ CPU solver (the FP64-promoted build oracle/_ref/ref64, compiled in place from
 the reference sources by oracle/Makefile) on seeded inputs.
 
 Run from the repository root on a machine that has the reference sources:
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [case ...]
+(with case names, only those cases are regenerated and merged into cases.json)
 
 Writes:
   hardcoded_coeff.txt, hardcoded_coeff2.txt, matrices.txt
@@ -54,6 +55,27 @@ def cases():
     lin["EVALUATE_SPONGE"] = 0
     out["n4_linear_nodiff"] = (lin, 5, False)
     out["n7_e222"] = (pulse(5, (2, 2, 2), 7), 3, False)
+
+    # N = 4 with the physics of the 64^3 tone-burst workload: nonlinear flux
+    # (B/A = 5), LDG diffusion and 2-element sponges on every face.
+    def full4(seed, ne, centre, diff_const=None):
+        cfg = W.gaussian_pulse(seed=seed, num_elements=ne, order=4, width=1.25, sponge=2)
+        cfg["IC_CENTER_X"], cfg["IC_CENTER_Y"], cfg["IC_CENTER_Z"] = centre
+        if diff_const is not None:
+            cfg["DIFF_CONST"] = diff_const
+        cfg["DT"] = W.cfl_dt(cfg)
+        return cfg
+
+    out["n4_full_e654"] = (full4(6, (6, 5, 4), (0.0, 0.0, 0.0)), 10, False)
+    # off centre, with velocity and a diffusivity large enough that the LDG
+    # terms move the result far above the 1e-10 bound, so every face and the
+    # diffusion operator carry data
+    off = full4(7, (6, 5, 4), (1.1, -0.7, 0.6), diff_const=2e-3)
+    off["IC_VX_AMPLITUDE"], off["IC_VY_AMPLITUDE"], off["IC_VZ_AMPLITUDE"] = -0.0008, 0.0005, 0.001
+    out["n4_full_offcentre"] = (off, 10, False)
+    n6 = pulse(8, (3, 3, 3), 6)
+    n6["DIFF_CONST"] = 2e-3
+    out["n6_e333"] = (n6, 4, False)
     return out
 
 
@@ -72,14 +94,20 @@ def run_ref(binary, cfg, steps, basis, work):
     return np.array(rho), np.array(vel), t, os.path.join(work, "params.txt")
 
 
-def main():
+def main(only=None):
     ref64 = os.path.join(ROOT, "oracle", "_ref", "ref64")
     ref32 = os.path.join(ROOT, "oracle", "_ref", "ref32")
     refinputs.write_coeff_files(HERE)
     refinputs.write_matrices(HERE)
     manifest = {}
+    mpath = os.path.join(HERE, "cases.json")
+    if only and os.path.exists(mpath):
+        with open(mpath) as f:
+            manifest = json.load(f)
     with tempfile.TemporaryDirectory() as tmp:
         for name, (cfg, steps, with32) in cases().items():
+            if only and name not in only:
+                continue
             rho, vel, t, pf = run_ref(ref64, cfg, steps, HERE, os.path.join(tmp, name))
             shutil.copy(pf, os.path.join(HERE, name + ".params.txt"))
             extra = {}
@@ -90,9 +118,10 @@ def main():
                                 steps=steps, **extra)
             manifest[name] = dict(steps=steps, dt=cfg["DT"], cfg={k: v for k, v in cfg.items()})
             print(name, rho.shape, "max|drho| %.6g" % np.abs(rho).max(), flush=True)
-    with open(os.path.join(HERE, "cases.json"), "w") as f:
+    with open(mpath, "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":
-    main()
+    # optional case names: regenerate only those and keep the other entries
+    main(set(sys.argv[1:]) or None)
