@@ -86,16 +86,6 @@ def build(verbose: bool = False, driver: bool = True) -> str:
     return LIB
 
 
-def run_peak_probe() -> str:
-    """Build and run csrc/probe/peak_probe.cu (FP64/FP32 FMA and copy throughput)."""
-    exe = os.path.join(PKG, "bin", "peak_probe")
-    os.makedirs(os.path.dirname(exe), exist_ok=True)
-    subprocess.check_call(["nvcc"] + ARCH + ["-O3", "-o", exe, os.path.join(CSRC, "probe", "peak_probe.cu")])
-    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
-    print(out)
-    return out
-
-
 if __name__ == "__main__":
     import sys
     print(build(verbose="-v" in sys.argv))

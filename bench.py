@@ -171,7 +171,7 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-FP64_PEAK_TFLOPS = 1.19  # FP64 FMA throughput measured on a GB300 (profiles/fp64_fp32_peak_probe.md)
+FP64_PEAK_TFLOPS = 1.19  # FP64 FMA throughput measured on a GB300 (8 independent DFMA chains per thread, all SMs)
 
 # Algorithmic HBM bytes per DOF-stage-update of the FP32 increment form with diffusion (4 DOFs per
 # node): stage kernel (11 + 15 + 23) / 3 values of 4 B per node over the three stages (input u, d,
