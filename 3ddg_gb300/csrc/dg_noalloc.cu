@@ -13,12 +13,18 @@
 // node), lives in a file-scope static device array instead of an allocation:
 // every GPU that loads this library holds it (27 MiB) until the process exits.
 // Its device address is looked up once per device with cudaGetSymbolAddress
-// (host code cannot use the array's name as a device address).  Every call
-// shares the array and it keeps the last call's contents: the gradient part is
-// fully rewritten by each call before it is read, the boundary-flag part is
-// cleared by each call, and calls whose work overlaps on the same GPU (for
-// example calls issued to two streams with no ordering between them) race on
-// it.
+// (host code cannot use the array's name as a device address).  With CUDA's
+// default lazy module loading that first look-up also loads this file's
+// device code on the device, and the 27 MiB is taken then: a host that
+// budgets device memory makes one call per device at start-up, before it
+// commits its own arena.  The address is cached for the life of the process,
+// so a cudaDeviceReset of a device invalidates it (this entry point is not
+// for processes that reset devices while it is loaded).  Every call shares the
+// array and it keeps the last call's contents: the gradient part is fully
+// rewritten by each call before it is read, the boundary-flag part is cleared
+// by each call, the operator part is rewritten by each call, and calls whose
+// work overlaps on the same GPU (for example calls issued to two streams with
+// no ordering between them) race on it.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -106,6 +112,25 @@ bool line_operators_stack(int K, const double* M, const double* S, double* D, do
     return true;
 }
 
+// Writes the two per-launch operator blocks into the scratch.  They travel as
+// kernel arguments, which the launch copies, so nothing is read from the
+// caller's host stack after this function returns.
+template <int K>
+__global__ void store_operators_kernel(dg::OpConst<double, K>* __restrict__ dst, const dg::OpConst<double, K> C,
+                                       const dg::OpConst<double, K> G)
+{
+    static_assert(sizeof(dg::OpConst<double, K>) % sizeof(int) == 0, "operator block size");
+    constexpr int NW = (int)(sizeof(dg::OpConst<double, K>) / sizeof(int));
+    const int* c = reinterpret_cast<const int*>(&C);
+    const int* g = reinterpret_cast<const int*>(&G);
+    int* d0 = reinterpret_cast<int*>(dst);
+    int* d1 = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dst) + kConstSlot);
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) {
+        d0[i] = c[i];
+        d1[i] = g[i];
+    }
+}
+
 template <int K>
 cudaError_t launch(const dg_params& p, const double* D, const double* L0, const double* LN,
                    const dg::StageIO<double>& io, const dg::MeshDev<double>& md, unsigned char* consts,
@@ -116,10 +141,7 @@ cudaError_t launch(const dg_params& p, const double* D, const double* L0, const 
                                                                      p.b_over_a, p.diff_const);
     const dg::OpConst<double, K> G =
         dg::make_grad_const<double, K>(D, L0, LN, p.elem_width, p.rho0, p.c0, p.diff_const);
-    // stream-ordered copies from the stack (staged by the runtime before return)
-    cudaError_t e = cudaMemcpyAsync(consts, &C, sizeof C, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(consts + kConstSlot, &G, sizeof G, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
+    store_operators_kernel<K><<<1, 128, 0, st>>>((dg::OpConst<double, K>*)consts, C, G);
     const dg::OpConst<double, K>* Cd = (const dg::OpConst<double, K>*)consts;
     const dg::OpConst<double, K>* Gd = (const dg::OpConst<double, K>*)(consts + kConstSlot);
     dim3 block(dg::npt_of(K), dg::epb_of(K));

@@ -148,8 +148,9 @@ int dg_eval_rhs(dg_handle* h, double* drho, double* vel);
  * buffers it owns: d_state (4 FP64 fields drho, u_x, u_y, u_z, element-major:
  * field f, element e, node n at f*n_elem*NP + e*NP + n, node n = (i*K+j)*K+k),
  * d_nbr (n_elem x 6 face table in the order -X +X -Y +Y -Z +Z: a neighbour
- * element index, or -1 - slot with slot < 6*n_elem for a boundary face, whose
- * exterior state is zero), d_sigma (n_elem sponge sigmas; may be NULL when
+ * element index in [0, n_elem), or -1 - slot with slot < 6*n_elem, i.e. a
+ * value in [-6*n_elem, -1], for a boundary face, whose exterior state is zero;
+ * the table is not checked, and any other entry is undefined behaviour), d_sigma (n_elem sponge sigmas; may be NULL when
  * eval_sponge is 0) and d_rhs (output, same layout as d_state); host mass and
  * stiff are the (N+1)^2 unit-interval matrices of matrices.txt.  FP64 only,
  * order 1..7, at most DG_NOALLOC_MAX_ELEMENTS elements and
@@ -158,7 +159,12 @@ int dg_eval_rhs(dg_handle* h, double* drho, double* vel);
  * the LDG-gradient scratch is a 27 MiB static device array that every GPU
  * loading this library holds until exit.  The first call on a device looks up
  * that array's address (cudaGetSymbolAddress), so make it before any stream
- * capture.  Calls share the scratch: calls whose work overlaps on one GPU race.
+ * capture; with CUDA's lazy module loading that call is also when the 27 MiB
+ * is taken on the device, so a host with a budgeted device arena makes one
+ * call per device at start-up, before committing its arena.  The address is
+ * kept for the process's life: a cudaDeviceReset while the library is loaded
+ * leaves it stale.  Calls share the scratch: calls whose work overlaps on one
+ * GPU race.
  * Asynchronous on ``stream`` (a cudaStream_t, NULL = the default stream). */
 int dg_eval_rhs_noalloc(const dg_params* p, const double* mass, const double* stiff,
                         const double* d_state, const int* d_nbr, const double* d_sigma,
