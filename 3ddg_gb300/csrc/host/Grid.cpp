@@ -17,6 +17,7 @@ struct Sim {
     int X = 0, Y = 0, Z = 0;
     std::vector<double> rho, vel, coords;  // host mirror [X][Y][Z], [3][X][Y][Z]
     bool coords_valid = false;
+    Matrix mass, stiff;                    // unit-interval M and S the simulation was created with
     ~Sim()
     {
         if (h) dg_destroy(h);
@@ -252,6 +253,13 @@ void Grid::init(const dg_params& p, const string& matrixFilename, Basis* basisPt
     const char* cf = (basisPtr && !basisPtr->coeffFile().empty()) ? basisPtr->coeffFile().c_str() : nullptr;
     sim->check(dg_create(&p, mf, cf, &sim->h), "dg_create");
     sim->check(dg_dims(sim->h, &sim->X, &sim->Y, &sim->Z), "dg_dims");
+    const int K = p.order + 1;
+    std::vector<double> m((size_t)K * K), st((size_t)K * K);
+    sim->check(dg_line_operators(p.order, p.lumped_mass, mf, cf, m.data(), st.data(), nullptr, nullptr, nullptr,
+                                 nullptr),
+               "dg_line_operators");
+    sim->mass = Matrix(K, K, m.data());
+    sim->stiff = Matrix(K, K, st.data());
     mOrder = p.order;
     for (int a = 0; a < 3; a++) {
         mNumElements[a] = p.num_elements[a];
@@ -350,6 +358,10 @@ void Grid::syncToDevice()
 }
 
 dg_handle* Grid::handle() { return sim->h; }
+
+Matrix* Grid::getMass() { return &sim->mass; }
+
+Matrix* Grid::getStiff() { return &sim->stiff; }
 
 double Grid::time() const { return dg_time(sim->h); }
 

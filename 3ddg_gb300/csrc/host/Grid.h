@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "BCParam.h"
+#include "Matrix.h"
 #include "dg3d.h"
 
 using std::ofstream;
@@ -109,6 +110,11 @@ public:
     int* getNumBlocks() { return mNumBlocks; }
     int* getNumElements() { return mNumElements; }
     int getOrder() const { return mOrder; }
+    // The unit-interval mass and stiffness matrices of this order
+    // (cppsrc/Grid.h:46-47), shared by the copies of this Grid; read-only
+    // (see Matrix.h).
+    Matrix* getMass();
+    Matrix* getStiff();
     void setZero();
     string getLayout();
     string allDRhoToString(bool twoDOnly);
