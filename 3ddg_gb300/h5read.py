@@ -1,11 +1,13 @@
 """Minimal pure-Python HDF5 reader for snapshot files.
 
 Reads files whose root group is an old-style symbol-table group (superblock
-version 0 or 1, version-1 object headers, v1 group B-tree, local heap,
-symbol-table nodes) holding contiguous, uncompressed numeric datasets: the
-layout of the reference's output files (cppsrc/HDF5Functions.cpp:249-397, one
-float64 dataset plus "time" per file) and of this package's writer.  For
-environments without h5py.
+version 0 or 1 at offset 0 or after a user block of 512, 1024, ... bytes,
+version-1 object headers with continuation blocks, v1 group B-tree, local
+heap, symbol-table nodes) holding contiguous or compact, uncompressed numeric
+datasets (data layout message versions 1, 2 and 3): the layout of the
+reference's output files (cppsrc/HDF5Functions.cpp:249-397, one float64
+dataset plus "time" per file), of this package's writer and of the HDF5
+library's default format.  For environments without h5py.
 """
 from __future__ import annotations
 
@@ -23,20 +25,24 @@ class H5FormatError(ValueError):
 
 class _File:
     def __init__(self, buf: bytes):
-        self.b = buf
-        if buf[:8] != SIG:
+        sb = 0  # the superblock sits at 0, 512, 1024, 2048, ...
+        while sb + 8 <= len(buf) and buf[sb:sb + 8] != SIG:
+            sb = 2 * sb if sb else 512
+        if sb + 8 > len(buf):
             raise H5FormatError("not an HDF5 file (signature)")
-        ver = buf[8]
+        ver = buf[sb + 8]
         if ver not in (0, 1):
             raise H5FormatError("superblock version %d not supported" % ver)
-        self.so, self.sl = buf[13], buf[14]
+        self.so, self.sl = buf[sb + 13], buf[sb + 14]
         if (self.so, self.sl) != (8, 8):
             raise H5FormatError("only 8-byte offsets/lengths supported")
-        off = 24 + (4 if ver == 1 else 0)
+        off = sb + 24 + (4 if ver == 1 else 0)
         base, _fs, eof, _drv = struct.unpack_from("<4Q", buf, off)
         self.eof = eof
         ent = off + 32
         _name, self.root_oh = struct.unpack_from("<2Q", buf, ent)
+        # every address in the file is relative to the base address
+        self.b = buf[base:]
 
     def u(self, fmt, off):
         return struct.unpack_from("<" + fmt, self.b, off)
@@ -46,11 +52,16 @@ class _File:
         if b[addr] != 1:
             raise H5FormatError("object header version %d not supported" % b[addr])
         nmsg, _ref, size = struct.unpack_from("<HII", b, addr + 2)
-        p, end, out = addr + 16, addr + 16 + size, []
-        while p + 8 <= end and len(out) < nmsg:
-            mtype, msize, _flags = struct.unpack_from("<HHB", b, p)
-            out.append((mtype, p + 8, msize))
-            p += 8 + msize
+        blocks, out = [(addr + 16, size)], []
+        while blocks and len(out) < nmsg:
+            p, n = blocks.pop(0)
+            end = p + n
+            while p + 8 <= end and len(out) < nmsg:
+                mtype, msize, _flags = struct.unpack_from("<HHB", b, p)
+                if mtype == 0x10:  # continuation: another block of messages
+                    blocks.append(struct.unpack_from("<2Q", b, p + 8))
+                out.append((mtype, p + 8, msize))
+                p += 8 + msize
         return out
 
     def group_entries(self, oh_addr):
@@ -108,16 +119,38 @@ class _File:
                 else:
                     raise H5FormatError("datatype class %d not supported" % cls)
             elif mtype == 0x0008:
-                ver, cls = self.b[p], self.b[p + 1]
-                if ver != 3 or cls != 1:
-                    raise H5FormatError("only contiguous layout (message v3) supported")
-                layout = self.u("2Q", p + 2)
+                ver = self.b[p]
+                if ver == 3:
+                    cls = self.b[p + 1]
+                    if cls == 1:  # contiguous: address, size
+                        layout = self.u("2Q", p + 2)
+                    elif cls == 0:  # compact: size, data in the message
+                        layout = (("compact", p + 4), self.u("H", p + 2)[0])
+                    else:
+                        raise H5FormatError("chunked or virtual layout not supported")
+                elif ver in (1, 2):
+                    nd, cls = self.b[p + 1], self.b[p + 2]
+                    if cls == 1:  # contiguous: address, then nd dimension sizes
+                        layout = (self.u("Q", p + 8)[0], None)
+                    elif cls == 0:  # compact: nd dimension sizes, size, data
+                        q = p + 8 + 4 * nd
+                        layout = (("compact", q + 4), self.u("I", q)[0])
+                    else:
+                        raise H5FormatError("chunked layout not supported")
+                else:
+                    raise H5FormatError("layout message version %d not supported" % ver)
+            elif mtype == 0x000B:
+                raise H5FormatError("filtered (compressed) datasets not supported")
         if dims is None or dtype is None or layout is None:
             raise H5FormatError("incomplete dataset header")
         addr, size = layout
         n = int(np.prod(dims)) if dims else 1
-        if size != n * dtype.itemsize or addr == UNDEF:
+        if size is not None and size != n * dtype.itemsize:
             raise H5FormatError("dataset size mismatch")
+        if isinstance(addr, tuple):
+            addr = addr[1]
+        elif addr == UNDEF:
+            return np.zeros(dims, dtype=dtype)  # unallocated: the default fill value
         return np.frombuffer(self.b, dtype=dtype, count=n, offset=addr).reshape(dims).copy()
 
 

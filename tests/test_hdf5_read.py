@@ -190,3 +190,30 @@ def test_hdf5input_error_codes(tmp_path, hdf5input_bin, case, code, msg):
         dims = ("2", "2", "3")
     out = subprocess.run([hdf5input_bin, path, name, *dims], capture_output=True, text=True).stdout
     assert msg in out and ("rc=%d" % code) in out
+
+
+def scipy_matlab_data():
+    """scipy's MATLAB test data: testhdf5_7.4_GLNX86.mat is an HDF5 file
+    written by the HDF5 library (MATLAB's, with a 512-byte user block and a
+    version-2 data layout message) holding the 1 x 9 double "testdouble";
+    testdouble_7.1_GLNX86.mat holds the same variable in MATLAB's own v5
+    format, which scipy.io.loadmat decodes without any HDF5 code."""
+    sio = pytest.importorskip("scipy.io")
+    d = os.path.join(os.path.dirname(sio.matlab.__file__), "tests", "data")
+    h5, v5 = os.path.join(d, "testhdf5_7.4_GLNX86.mat"), os.path.join(d, "testdouble_7.1_GLNX86.mat")
+    if not (os.path.exists(h5) and os.path.exists(v5)):
+        pytest.skip("scipy's MATLAB test data is not installed")
+    return h5, sio.loadmat(v5)["testdouble"]
+
+
+def test_readers_read_a_file_written_by_the_hdf5_library():
+    """Both readers (dg_hdf5_read and the Python h5read) on a file that the
+    HDF5 library wrote, against an independent decoder of the same values."""
+    import importlib
+    h5path, want = scipy_matlab_data()
+    m = dg()
+    a, cls = m.hdf5_read(h5path, "testdouble")
+    assert cls == 1 and a.shape == (9, 1)  # MATLAB stores the 1 x 9 array column-major
+    assert np.array_equal(a.T, want)
+    b = importlib.import_module("3ddg_gb300.h5read").read(h5path)["testdouble"]
+    assert np.array_equal(b, a)
