@@ -120,6 +120,7 @@ def lib():
             "dg_serve_run": (i, [vp, d]),
             "dg_serve_result": (i, [vp, C.c_longlong, C.POINTER(d), C.POINTER(d), C.POINTER(d), vp, vp]),
             "dg_serve_stats": (i, [vp, C.POINTER(i), C.POINTER(d), C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
+            "dg_serve_utilization": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
             "dg_write_basis_files": (i, [cp, i, i]),
             "dg_line_operators": (i, [i, i, cp, cp, vp, vp, vp, vp, vp, vp]),
         }
@@ -480,6 +481,13 @@ class Server:
                "dg_serve_stats")
         return {"completed": n.value, "p50_s": p50.value, "p99_s": p99.value, "solves_per_s": sps.value,
                 "mean_inflight": mi.value}
+
+    def utilization(self):
+        busy, span, work = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().dg_serve_utilization(self.h, C.byref(busy), C.byref(span), C.byref(work)),
+               "dg_serve_utilization")
+        return {"gpu_busy_s": busy.value, "span_s": span.value, "dof_stage_updates": work.value,
+                "busy_frac": busy.value / span.value if span.value > 0 else 0.0}
 
 
 def line_operators(order: int, lumped: bool = False, matrix_file=None, coeff_file=None):

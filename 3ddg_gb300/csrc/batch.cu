@@ -43,6 +43,9 @@ size_t batch_problem_bytes(const dg_params& p)
 
 namespace {
 
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t n) { return (n + kAlign - 1) / kAlign * kAlign; }
+
 template <int K>
 void fill_ops(BatchProblem& P, const LineOperators& op, const dg_params& p)
 {
@@ -70,6 +73,86 @@ void fill_ops(BatchProblem& P, const LineOperators& op, const dg_params& p)
 
 }  // namespace
 
+// ------------------------------------------------------------ PinnedPool
+PinnedPool::Block* PinnedPool::acquire(size_t bytes, std::string& err)
+{
+    std::lock_guard<std::mutex> lock(mu);
+    Block* best = nullptr;
+    for (auto& b : blocks) {
+        if (b->busy || b->cap < bytes) continue;
+        if (b->ev_pending) {
+            const cudaError_t q = cudaEventQuery(b->ev);
+            if (q == cudaErrorNotReady) {
+                (void)cudaGetLastError();
+                continue;
+            }
+            if (q != cudaSuccess) {
+                err = std::string("cudaEventQuery: ") + cudaGetErrorString(q);
+                return nullptr;
+            }
+            b->ev_pending = false;
+        }
+        if (!best || b->cap < best->cap) best = b.get();
+    }
+    if (!best) {
+        auto nb = std::make_unique<Block>();
+        const size_t mib = (size_t)1 << 20;
+        nb->cap = (std::max(bytes, mib) + mib - 1) / mib * mib;
+        cudaError_t e = cudaHostAlloc(&nb->ptr, nb->cap, cudaHostAllocPortable);
+        if (e != cudaSuccess) {
+            err = std::string("cudaHostAlloc: ") + cudaGetErrorString(e);
+            return nullptr;
+        }
+        e = cudaEventCreateWithFlags(&nb->ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaFreeHost(nb->ptr);
+            err = std::string("cudaEventCreate: ") + cudaGetErrorString(e);
+            return nullptr;
+        }
+        best = nb.get();
+        blocks.push_back(std::move(nb));
+    }
+    best->busy = true;
+    return best;
+}
+
+void PinnedPool::release(Block* b, cudaStream_t after)
+{
+    if (!b) return;
+    std::lock_guard<std::mutex> lock(mu);
+    b->ev_pending = cudaEventRecord(b->ev, after) == cudaSuccess;
+    if (!b->ev_pending) {
+        // the stream is unusable: keep the block out of circulation
+        (void)cudaGetLastError();
+        return;
+    }
+    b->busy = false;
+}
+
+void PinnedPool::release_now(Block* b)
+{
+    if (!b) return;
+    std::lock_guard<std::mutex> lock(mu);
+    b->busy = false;
+}
+
+PinnedPool::~PinnedPool()
+{
+    for (auto& b : blocks) {
+        if (b->ev) {
+            cudaEventSynchronize(b->ev);
+            cudaEventDestroy(b->ev);
+        }
+        if (b->ptr) cudaFreeHost(b->ptr);
+    }
+}
+
+Batch::Prepared::~Prepared()
+{
+    if (pool && host) pool->release_now(host);
+}
+
+// ------------------------------------------------------------ Batch
 std::string Batch::validate(const dg_params& p)
 {
     std::string err = validate_params(p);
@@ -108,45 +191,48 @@ int Batch::init(int device_capacity)
         }
     }
     ctas_per_sm = max_ctas_per_sm;
-    capacity = std::max(1, device_capacity);
-    DGB_CUDA(cudaMalloc(&d_probs, capacity * sizeof(BatchProblem)));
+    // a pool of this device's memory that keeps what is freed for reuse
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof props);
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    DGB_CUDA(cudaMemPoolCreate(&pool, &props));
+    unsigned long long keep = ~0ull;
+    DGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    capacity = std::max(16, device_capacity);
+    DGB_CUDA(cudaMallocFromPoolAsync((void**)&d_probs, capacity * sizeof(BatchProblem), pool, stream));
+    DGB_CUDA(cudaStreamSynchronize(stream));
     for (int k = 0; k <= BATCH_KMAX; k++) passes[k] = 4;
     return DG_OK;
 }
 
-int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file, const char* coeff_file, int* index)
+int Batch::prepare(const dg_params& p, double dt, int steps, const char* matrix_file, const char* coeff_file,
+                   Prepared& out)
 {
     std::string err = validate(p);
     if (!err.empty()) return fail(DG_ERR_INVALID, err);
     if (!(dt > 0.0) || steps < 1) return fail(DG_ERR_INVALID, "batch: dt must be > 0 and steps >= 1");
-    if ((int)probs.size() >= capacity) {
-        // grow the descriptor array
-        int ncap = capacity * 2;
-        BatchProblem* nd = nullptr;
-        DGB_CUDA(cudaMalloc(&nd, ncap * sizeof(BatchProblem)));
-        DGB_CUDA(cudaMemcpyAsync(nd, d_probs, probs.size() * sizeof(BatchProblem), cudaMemcpyDeviceToDevice, stream));
-        DGB_CUDA(cudaStreamSynchronize(stream));
-        cudaFree(d_probs);
-        d_probs = nd;
-        capacity = ncap;
-    }
     LineOperators op;
     const std::string key = std::to_string(p.order) + "|" + std::to_string(p.lumped_mass) + "|" +
                             (matrix_file ? matrix_file : "") + "|" + (coeff_file ? coeff_file : "");
-    auto it = op_cache.find(key);
-    if (it == op_cache.end()) {
-        err = build_line_operators(p.order, p.lumped_mass != 0, matrix_file ? matrix_file : "",
-                                   coeff_file ? coeff_file : "", op);
-        if (!err.empty()) return fail(err.find("Opening") == 0 ? DG_ERR_IO : DG_ERR_INVALID, err);
-        op_cache[key] = op;
-    } else {
-        op = it->second;
+    {
+        std::lock_guard<std::mutex> lock(op_mu);
+        auto it = op_cache.find(key);
+        if (it == op_cache.end()) {
+            err = build_line_operators(p.order, p.lumped_mass != 0, matrix_file ? matrix_file : "",
+                                       coeff_file ? coeff_file : "", op);
+            if (!err.empty()) return fail(err.find("Opening") == 0 ? DG_ERR_IO : DG_ERR_INVALID, err);
+            op_cache[key] = op;
+        } else {
+            op = it->second;
+        }
     }
     MeshHost m;
-    err = build_mesh(p, op, m);
+    err = build_mesh(p, op, m, false);
     if (!err.empty()) return fail(DG_ERR_INVALID, err);
 
-    Entry E;
+    Entry& E = out.E;
     E.op_key = key;
     E.p = p;
     E.dt = dt;
@@ -154,22 +240,33 @@ int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file
     E.K = m.K;
     E.np = m.NP;
     E.n_elem = m.n_elem;
-    for (int a = 0; a < 3; a++) E.dims[a] = m.E[a] * m.K;
+    for (int a = 0; a < 3; a++) {
+        E.dims[a] = m.E[a] * m.K;
+        E.nb[a] = m.nb[a];
+        E.ne[a] = m.ne[a];
+    }
     E.fs = m.fstride();
-    E.nb[0] = m.nb[0]; E.nb[1] = m.nb[1]; E.nb[2] = m.nb[2];
-    E.ne[0] = m.ne[0]; E.ne[1] = m.ne[1]; E.ne[2] = m.ne[2];
-    const size_t bytes = E.fs * 23 * sizeof(float);
-    DGB_CUDA(cudaMalloc(&E.data, bytes));
-    DGB_CUDA(cudaMemsetAsync(E.data, 0, bytes, stream));
-    std::vector<int> nbr(m.nbr.size());
-    for (size_t i = 0; i < m.nbr.size(); i++) nbr[i] = m.nbr[i] >= 0 ? m.nbr[i] : -1 - m.bnd_face[-1 - m.nbr[i]];
-    DGB_CUDA(cudaMalloc(&E.nbr, nbr.size() * sizeof(int)));
-    DGB_CUDA(cudaMemcpyAsync(E.nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-    std::vector<float> sg(m.sigma.begin(), m.sigma.end());
-    DGB_CUDA(cudaMalloc(&E.sigma, sg.size() * sizeof(float)));
-    DGB_CUDA(cudaMemcpyAsync(E.sigma, sg.data(), sg.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
-    std::vector<float> s0(m.state0.begin(), m.state0.end());
-    DGB_CUDA(cudaMemcpyAsync(E.data, s0.data(), s0.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+    out.data_bytes = align_up(E.fs * 23 * sizeof(float));
+    out.nbr_bytes = align_up(m.nbr.size() * sizeof(int));
+    E.chunk_bytes = out.data_bytes + out.nbr_bytes + align_up(m.sigma.size() * sizeof(float));
+
+    // page-locked staging: nbr | sigma | [state0]
+    out.has_state0 = !m.state0.empty();
+    out.sigma_off = out.nbr_bytes;
+    out.state_off = out.sigma_off + align_up(m.sigma.size() * sizeof(float));
+    const size_t hbytes = out.state_off + (out.has_state0 ? 4 * E.fs * sizeof(float) : 0);
+    out.pool = &pinned;
+    out.host = pinned.acquire(hbytes, err);
+    if (!out.host) return fail(DG_ERR_CUDA, "batch: " + err);
+    unsigned char* h = (unsigned char*)out.host->ptr;
+    int* hn = (int*)h;
+    for (size_t i = 0; i < m.nbr.size(); i++) hn[i] = m.nbr[i] >= 0 ? m.nbr[i] : -1 - m.bnd_face[-1 - m.nbr[i]];
+    float* hs = (float*)(h + out.sigma_off);
+    for (size_t i = 0; i < m.sigma.size(); i++) hs[i] = (float)m.sigma[i];
+    if (out.has_state0) {
+        float* h0 = (float*)(h + out.state_off);
+        for (size_t i = 0; i < 4 * E.fs; i++) h0[i] = (float)m.state0[i];
+    }
 
     BatchProblem& P = E.desc;
     std::memset(&P, 0, sizeof P);
@@ -180,15 +277,6 @@ int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file
     P.active = 1;
     P.cur = 0;
     P.steps_left = steps;
-    float* base = (float*)E.data;
-    P.u[0] = base;
-    P.u[1] = base + 4 * E.fs;
-    P.comp = base + 8 * E.fs;
-    P.d[0] = base + 12 * E.fs;
-    P.d[1] = base + 16 * E.fs;
-    P.q = base + 20 * E.fs;
-    P.nbr = E.nbr;
-    P.sigma = E.sigma;
     P.fs = E.fs;
     switch (m.K) {
     case 2: fill_ops<2>(P, op, p); break;
@@ -223,36 +311,111 @@ int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file
     P.src_freq = p.src_freq;
     P.src_T = p.src_face >= 0 ? p.src_cycles / p.src_freq : 0.0;
     P.src_phase = p.src_phase;
+    return DG_OK;
+}
+
+int Batch::commit(Prepared& pr, int* index)
+{
+    if (!pr.host) return fail(DG_ERR_STATE, "batch: problem not prepared");
+    Entry E = pr.E;
+    int slot;
+    if (!free_slots.empty()) {
+        slot = free_slots.back();
+        free_slots.pop_back();
+    } else {
+        if (slot_hi >= capacity) {
+            // grow the descriptor array in stream order
+            const int ncap = capacity * 2;
+            BatchProblem* nd = nullptr;
+            DGB_CUDA(cudaMallocFromPoolAsync((void**)&nd, ncap * sizeof(BatchProblem), pool, stream));
+            DGB_CUDA(cudaMemcpyAsync(nd, d_probs, slot_hi * sizeof(BatchProblem), cudaMemcpyDeviceToDevice, stream));
+            DGB_CUDA(cudaFreeAsync(d_probs, stream));
+            d_probs = nd;
+            capacity = ncap;
+            graph_stale = true;
+        }
+        slot = slot_hi++;
+    }
+    DGB_CUDA(cudaMallocFromPoolAsync(&E.chunk, E.chunk_bytes, pool, stream));
+    unsigned char* c = (unsigned char*)E.chunk;
+    E.data = c;
+    E.nbr = (int*)(c + pr.data_bytes);
+    E.sigma = (float*)(c + pr.data_bytes + pr.nbr_bytes);
+    const unsigned char* h = (const unsigned char*)pr.host->ptr;
+    DGB_CUDA(cudaMemsetAsync(E.data, 0, E.fs * 23 * sizeof(float), stream));
+    DGB_CUDA(cudaMemcpyAsync(E.nbr, h, (size_t)E.n_elem * 6 * sizeof(int), cudaMemcpyHostToDevice, stream));
+    DGB_CUDA(cudaMemcpyAsync(E.sigma, h + pr.sigma_off, (size_t)E.n_elem * sizeof(float), cudaMemcpyHostToDevice,
+                             stream));
+    if (pr.has_state0)
+        DGB_CUDA(cudaMemcpyAsync(E.data, h + pr.state_off, 4 * E.fs * sizeof(float), cudaMemcpyHostToDevice, stream));
+    pinned.release(pr.host, stream);
+    pr.host = nullptr;
+
+    BatchProblem& P = E.desc;
+    float* base = (float*)E.data;
+    P.u[0] = base;
+    P.u[1] = base + 4 * E.fs;
+    P.comp = base + 8 * E.fs;
+    P.d[0] = base + 12 * E.fs;
+    P.d[1] = base + 16 * E.fs;
+    P.q = base + 20 * E.fs;
+    P.nbr = E.nbr;
+    P.sigma = E.sigma;
+    batch_set_problem<<<1, 128, 0, stream>>>(d_probs + slot, P);
+    DGB_CUDA(cudaGetLastError());
+    E.slot = slot;
     E.id = next_id++;
     probs.push_back(E);
-    DGB_CUDA(cudaMemcpyAsync(d_probs + probs.size() - 1, &P, sizeof P, cudaMemcpyHostToDevice, stream));
-    DGB_CUDA(cudaStreamSynchronize(stream));
     if (index) *index = (int)probs.size() - 1;
     tiles_dirty = true;
     return DG_OK;
 }
 
+int Batch::add(const dg_params& p, double dt, int steps, const char* matrix_file, const char* coeff_file, int* index)
+{
+    Prepared pr;
+    int rc = prepare(p, dt, steps, matrix_file, coeff_file, pr);
+    if (rc) return rc;
+    return commit(pr, index);
+}
+
 int Batch::remove(int i)
 {
     if (i < 0 || i >= (int)probs.size()) return fail(DG_ERR_INVALID, "batch: bad problem index");
-    DGB_CUDA(cudaStreamSynchronize(stream));
     Entry& E = probs[i];
-    cudaFree(E.data);
-    cudaFree(E.nbr);
-    cudaFree(E.sigma);
+    BatchProblem off;
+    std::memset(&off, 0, sizeof off);
+    batch_set_problem<<<1, 128, 0, stream>>>(d_probs + E.slot, off);
+    DGB_CUDA(cudaGetLastError());
+    DGB_CUDA(cudaFreeAsync(E.chunk, stream));
+    free_slots.push_back(E.slot);
     probs.erase(probs.begin() + i);
-    // re-pack the descriptor array (host copies are authoritative except the
-    // time-dependent fields, which are read back first)
-    std::vector<BatchProblem> h(probs.size());
-    for (size_t j = 0; j < probs.size(); j++) h[j] = probs[j].desc;
-    if (!h.empty()) {
-        // pull the live descriptors of the kept problems, in their old slots
-        std::vector<BatchProblem> live(probs.size() + 1);
-        DGB_CUDA(cudaMemcpy(live.data(), d_probs, (probs.size() + 1) * sizeof(BatchProblem), cudaMemcpyDeviceToHost));
-        for (size_t j = 0; j < probs.size(); j++) h[j] = live[j < (size_t)i ? j : j + 1];
-        DGB_CUDA(cudaMemcpy(d_probs, h.data(), h.size() * sizeof(BatchProblem), cudaMemcpyHostToDevice));
-    }
     tiles_dirty = true;
+    return DG_OK;
+}
+
+int Batch::enqueue_state_copy(int i, long long steps_done, PinnedPool::Block* dst)
+{
+    if (i < 0 || i >= (int)probs.size()) return fail(DG_ERR_INVALID, "batch: bad problem index");
+    const Entry& E = probs[i];
+    const size_t g = (size_t)E.n_elem * E.K * E.K * E.K;
+    if (!dst || dst->cap < 4 * g * sizeof(double)) return fail(DG_ERR_INVALID, "batch: result block too small");
+    double* st = nullptr;
+    DGB_CUDA(cudaMallocFromPoolAsync((void**)&st, 4 * g * sizeof(double), pool, stream));
+    GridMap gm;
+    gm.K = E.K;
+    for (int a = 0; a < 3; a++) {
+        gm.nb[a] = E.nb[a];
+        gm.ne[a] = E.ne[a];
+        gm.E[a] = E.nb[a] * E.ne[a];
+    }
+    gm.elem_per_block = E.ne[0] * E.ne[1] * E.ne[2];
+    // the state ping-pongs once per step, starting in u[0]
+    const float* u = E.desc.u[steps_done & 1];
+    pack_grid_kernel<float><<<304, 256, 0, stream>>>(u, E.fs, E.np, 4, gm, E.n_elem, st, g);
+    DGB_CUDA(cudaGetLastError());
+    DGB_CUDA(cudaMemcpyAsync(dst->ptr, st, 4 * g * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    DGB_CUDA(cudaFreeAsync(st, stream));
     return DG_OK;
 }
 
@@ -282,7 +445,7 @@ void Batch::build_tiles()
         const int chunk = bepb_of(K) * std::max(1, passes[K]);
         for (int e0 = 0; e0 < E.n_elem; e0 += chunk) {
             BatchTile t;
-            t.prob = i;
+            t.prob = E.slot;
             t.e0 = e0;
             t.count = std::min(chunk, E.n_elem - e0);
             t.K = K;
@@ -292,38 +455,47 @@ void Batch::build_tiles()
     }
 }
 
+// Rebuild the tile list and upload it in stream order (after the steps
+// already enqueued, which read the previous list); no synchronisation.
 int Batch::upload_tiles()
 {
     build_tiles();
-    if ((int)groups.size() > counter_groups) {
+    const int G = (int)groups.size();
+    if (G > counter_groups) {
         // tile counters: [stage][group][phase]
-        DGB_CUDA(cudaStreamSynchronize(stream));
-        if (d_counters) cudaFree(d_counters);
-        d_counters = nullptr;
-        counter_groups = 0;
-        DGB_CUDA(cudaMalloc(&d_counters, 3 * groups.size() * 2 * sizeof(int)));
-        counter_groups = (int)groups.size();
+        const int ng = std::max(G, std::max(8, 2 * counter_groups));
+        int* nc = nullptr;
+        DGB_CUDA(cudaMallocFromPoolAsync((void**)&nc, 3 * ng * 2 * sizeof(int), pool, stream));
+        if (d_counters) DGB_CUDA(cudaFreeAsync(d_counters, stream));
+        d_counters = nc;
+        counter_groups = ng;
     }
     if ((int)tiles.size() > tile_capacity) {
-        if (d_tiles) cudaFree(d_tiles);
-        tile_capacity = std::max<int>((int)tiles.size(), 2 * tile_capacity);
-        DGB_CUDA(cudaMalloc(&d_tiles, tile_capacity * sizeof(BatchTile)));
+        const int cap = std::max<int>((int)tiles.size(), 2 * tile_capacity);
+        BatchTile* nt = nullptr;
+        DGB_CUDA(cudaMallocFromPoolAsync((void**)&nt, cap * sizeof(BatchTile), pool, stream));
+        if (d_tiles) DGB_CUDA(cudaFreeAsync(d_tiles, stream));
+        d_tiles = nt;
+        tile_capacity = cap;
     }
-    if (!tiles.empty())
-        DGB_CUDA(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
-                                 stream));
-    DGB_CUDA(cudaStreamSynchronize(stream));
+    if (!tiles.empty()) {
+        std::string err;
+        PinnedPool::Block* b = pinned.acquire(tiles.size() * sizeof(BatchTile), err);
+        if (!b) return fail(DG_ERR_CUDA, "batch: " + err);
+        std::memcpy(b->ptr, tiles.data(), tiles.size() * sizeof(BatchTile));
+        cudaError_t e = cudaMemcpyAsync(d_tiles, b->ptr, tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
+                                        stream);
+        pinned.release(b, stream);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    }
     tiles_dirty = false;
-    if (graph) {
-        cudaGraphExecDestroy(graph);
-        graph = nullptr;
-    }
+    graph_stale = true;
     return DG_OK;
 }
 
 int Batch::launch_step()
 {
-    const int n = (int)probs.size();
+    const int n = slot_hi;
     const int G = (int)groups.size();
     DGB_CUDA(cudaMemsetAsync(d_counters, 0, 3 * G * 2 * sizeof(int), stream));
     batch_step_begin<<<(n + 127) / 128, 128, 0, stream>>>(d_probs, n);
@@ -383,7 +555,9 @@ int Batch::step(int nsteps)
         int rc = upload_tiles();
         if (rc) return rc;
     }
-    if (use_graph && !graph) {
+    if (use_graph && (graph_stale || !graph)) {
+        // capture the step; update the instantiated graph in place when its
+        // shape allows, else instantiate anew
         cudaGraph_t g = nullptr;
         DGB_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         const long long before = launches;
@@ -394,16 +568,29 @@ int Batch::step(int nsteps)
         if (rc || ec != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
             cudaGetLastError();
+            if (graph) cudaGraphExecDestroy(graph);
+            graph = nullptr;
             use_graph = false;  // capture unsupported here: launch directly
         } else {
-            cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
-            cudaGraphDestroy(g);
-            if (ei != cudaSuccess) {
-                graph = nullptr;
-                use_graph = false;
-                cudaGetLastError();
+            if (graph) {
+                cudaGraphExecUpdateResultInfo info;
+                if (cudaGraphExecUpdate(graph, g, &info) != cudaSuccess) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(graph);
+                    graph = nullptr;
+                }
             }
+            if (!graph) {
+                cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
+                if (ei != cudaSuccess) {
+                    graph = nullptr;
+                    use_graph = false;
+                    cudaGetLastError();
+                }
+            }
+            cudaGraphDestroy(g);
         }
+        graph_stale = false;
     }
     for (int i = 0; i < nsteps; i++) {
         if (graph) {
@@ -419,11 +606,11 @@ int Batch::step(int nsteps)
 
 int Batch::sync_descs()
 {
-    std::vector<BatchProblem> h(probs.size());
-    if (h.empty()) return DG_OK;
+    if (probs.empty()) return DG_OK;
+    std::vector<BatchProblem> h(slot_hi);
     DGB_CUDA(cudaMemcpyAsync(h.data(), d_probs, h.size() * sizeof(BatchProblem), cudaMemcpyDeviceToHost, stream));
     DGB_CUDA(cudaStreamSynchronize(stream));
-    for (size_t i = 0; i < h.size(); i++) probs[i].desc = h[i];
+    for (Entry& E : probs) E.desc = h[E.slot];
     return DG_OK;
 }
 
@@ -435,7 +622,7 @@ int Batch::get_state(int i, double* drho, double* vel)
     Entry& E = probs[i];
     const size_t g = (size_t)E.n_elem * E.K * E.K * E.K;
     double* st = nullptr;
-    DGB_CUDA(cudaMallocAsync(&st, 4 * g * sizeof(double), stream));
+    DGB_CUDA(cudaMallocFromPoolAsync((void**)&st, 4 * g * sizeof(double), pool, stream));
     GridMap gm;
     gm.K = E.K;
     for (int a = 0; a < 3; a++) {
@@ -473,10 +660,11 @@ int Batch::snapshot(std::vector<std::vector<char>>& save)
 
 int Batch::restore(const std::vector<std::vector<char>>& save)
 {
-    for (size_t i = 0; i < probs.size(); i++)
+    for (size_t i = 0; i < probs.size(); i++) {
         DGB_CUDA(cudaMemcpyAsync(probs[i].data, save[i].data(), save[i].size(), cudaMemcpyHostToDevice, stream));
-    DGB_CUDA(cudaMemcpyAsync(d_probs, saved_desc.data(), saved_desc.size() * sizeof(BatchProblem),
-                             cudaMemcpyHostToDevice, stream));
+        batch_set_problem<<<1, 128, 0, stream>>>(d_probs + probs[i].slot, saved_desc[i]);
+        DGB_CUDA(cudaGetLastError());
+    }
     DGB_CUDA(cudaStreamSynchronize(stream));
     for (size_t i = 0; i < probs.size(); i++) probs[i].desc = saved_desc[i];
     return DG_OK;
@@ -542,10 +730,7 @@ int Batch::autotune(int trial_steps, std::string& report)
         for (int c = 1; c <= max_ctas_per_sm; c++) {
             if (c == keep_c) continue;
             ctas_per_sm = c;
-            if (graph) {
-                cudaGraphExecDestroy(graph);
-                graph = nullptr;
-            }
+            graph_stale = true;
             double ms;
             if ((rc = restore(save))) return rc;
             if ((rc = time_steps(trial_steps, &ms))) return rc;
@@ -583,14 +768,14 @@ Batch::~Batch()
     }
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (graph) cudaGraphExecDestroy(graph);
-    for (Entry& E : probs) {
-        cudaFree(E.data);
-        cudaFree(E.nbr);
-        cudaFree(E.sigma);
+    if (stream) {
+        for (Entry& E : probs) cudaFreeAsync(E.chunk, stream);
+        if (d_probs) cudaFreeAsync(d_probs, stream);
+        if (d_tiles) cudaFreeAsync(d_tiles, stream);
+        if (d_counters) cudaFreeAsync(d_counters, stream);
+        cudaStreamSynchronize(stream);
     }
-    if (d_probs) cudaFree(d_probs);
-    if (d_tiles) cudaFree(d_tiles);
-    if (d_counters) cudaFree(d_counters);
+    if (pool) cudaMemPoolDestroy(pool);
     if (stream) cudaStreamDestroy(stream);
 }
 

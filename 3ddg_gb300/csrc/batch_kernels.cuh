@@ -373,6 +373,16 @@ __global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K, PHASE))
     }
 }
 
+// Writes one problem descriptor into its slot.  The descriptor travels as a
+// kernel argument (copied at launch), so the host needs no page-locked
+// staging and no synchronisation to add or retire a problem.
+__global__ void batch_set_problem(BatchProblem* __restrict__ dst, const BatchProblem P)
+{
+    const int* s = reinterpret_cast<const int*>(&P);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(BatchProblem) / sizeof(int)); i += blockDim.x) d[i] = s[i];
+}
+
 // Per-problem bookkeeping around a step (one thread per problem).
 __global__ void batch_step_begin(BatchProblem* probs, int n)
 {

@@ -129,7 +129,7 @@ size_t grid_offset(const MeshHost& m, int e, int n)
     return (ii * ((size_t)m.E[1] * K) + jj) * ((size_t)m.E[2] * K) + kk;
 }
 
-std::string build_mesh(const dg_params& p, const LineOperators& op, MeshHost& m)
+std::string build_mesh(const dg_params& p, const LineOperators& op, MeshHost& m, bool with_zero_state0)
 {
     std::string err = validate_params(p);
     if (!err.empty()) return err;
@@ -218,6 +218,10 @@ std::string build_mesh(const dg_params& p, const LineOperators& op, MeshHost& m)
     }
 
     // Initial condition in the device layout (threads over element ranges).
+    if (!ic_on && !with_zero_state0) {
+        m.state0.clear();
+        return "";
+    }
     m.state0.assign(4 * m.fstride(), 0.0);
     if (ic_on) {
         unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));

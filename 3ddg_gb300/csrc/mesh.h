@@ -45,7 +45,7 @@ struct MeshHost {
     std::vector<int> bnd_face;    // n_bnd: face 0..5
     std::vector<double> bnd_ic;   // n_bnd * 2 * K*K: exterior drho, u_normal of the IC halo
     std::vector<double> bnd_ap;   // n_bnd * K*K: source aperture weight (0 off the source face)
-    std::vector<double> state0;   // 4 * n_elem * NP: initial drho, u0, u1, u2
+    std::vector<double> state0;   // 4 * n_elem * NP: initial drho, u0, u1, u2 (empty: all zero)
 
     size_t fstride() const { return (size_t)n_elem * NP; }
     // global element coordinates of element e
@@ -56,7 +56,10 @@ struct MeshHost {
 };
 
 std::string validate_params(const dg_params& p);
-std::string build_mesh(const dg_params& p, const LineOperators& op, MeshHost& m);
+// With with_zero_state0 false, state0 is left empty when the initial
+// condition is zero everywhere (no Gaussian axis enabled): the caller clears
+// the state on the device instead of uploading zeros.
+std::string build_mesh(const dg_params& p, const LineOperators& op, MeshHost& m, bool with_zero_state0 = true);
 
 // Node-duplicated [X][Y][Z] position of node n of element e.
 size_t grid_offset(const MeshHost& m, int e, int n);

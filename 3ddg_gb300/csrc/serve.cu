@@ -10,9 +10,12 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -34,23 +37,136 @@ struct Server {
         int remaining = 0;
         std::vector<double> rho, vel;  // result (when kept)
         int dims[3] = {0, 0, 0};
+        // host preparation by the worker thread (fields guarded by mu)
+        std::unique_ptr<Batch::Prepared> prep;
+        bool prep_done = false;
+        int prep_rc = 0;
+        std::string prep_err;
+        PinnedPool::Block* result = nullptr;  // result copy in flight
     };
+    // One tick's device work: its RK steps between two timing events, then
+    // the retirements enqueued behind them (a third event).
+    struct TickRec {
+        cudaEvent_t start = nullptr, end = nullptr, post = nullptr;
+        int k = 0;
+        std::vector<long long> done;
+    };
+
     Batch batch;
     size_t budget = 0, in_use = 0;
     bool keep_results = false;
-    std::map<long long, Req> reqs;
-    std::deque<long long> pending;   // submitted, not yet arrived or not yet admitted (arrival order)
+    std::map<long long, Req> reqs;   // inserted only by submit (under mu)
+    std::deque<long long> pending;   // submitted, not yet admitted (arrival order)
     std::vector<long long> inflight; // batch index -> request id
+    std::deque<TickRec> outstanding; // ticks enqueued, not yet seen complete
+    std::vector<cudaEvent_t> timing_events, plain_events;
     long long next_id = 1;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    cudaEvent_t base_ev = nullptr;   // host time t_base on the device timeline
+    double t_base = 0.0;
     long long ticks = 0;
     double inflight_sum = 0.0;
-    double step_s = 0.0;  // running estimate of the wall time of one batch step
+    double step_s = 0.0;   // running estimate of the device time of one batch step
+    double busy_s = 0.0;   // device time in RK steps
+    double work = 0.0;     // DOF-stage updates enqueued
     static constexpr int kMaxStepsPerTick = 64;
+    static constexpr int kDepth = 2;          // ticks the host may run ahead of the device
+    static constexpr int kPrepareAhead = 64;  // requests prepared ahead of admission
+
+    // worker thread: builds arriving requests' meshes ahead of admission
+    std::mutex mu;
+    std::condition_variable cv_work, cv_ready;
+    std::deque<long long> to_prepare;  // arrival order
+    int prepared_ahead = 0;
+    bool stop = false;
+    std::thread worker;
 
     double now() const
     {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    int init(size_t budget_bytes, bool keep)
+    {
+        budget = budget_bytes;
+        keep_results = keep;
+        int rc = batch.init(64);
+        if (rc) return rc;
+        cudaError_t e = cudaEventCreate(&base_ev);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(batch.stream);
+        if (e == cudaSuccess) e = cudaEventRecord(base_ev, batch.stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(base_ev);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("dg_serve_create: ") + cudaGetErrorString(e));
+        t_base = now();
+        worker = std::thread([this]() { work_loop(); });
+        return DG_OK;
+    }
+
+    void work_loop()
+    {
+        cudaSetDevice(batch.device);
+        for (;;) {
+            Req* r = nullptr;
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                cv_work.wait(lock, [&] { return stop || (!to_prepare.empty() && prepared_ahead < kPrepareAhead); });
+                if (stop) return;
+                r = &reqs[to_prepare.front()];
+                to_prepare.pop_front();
+                prepared_ahead++;
+            }
+            auto pr = std::make_unique<Batch::Prepared>();
+            const int rc = batch.prepare(r->p, r->dt, r->steps, nullptr, nullptr, *pr);
+            const std::string err = rc ? dg_last_error() : "";
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                r->prep = std::move(pr);
+                r->prep_rc = rc;
+                r->prep_err = err;
+                r->prep_done = true;
+            }
+            cv_ready.notify_all();
+        }
+    }
+
+    ~Server()
+    {
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            stop = true;
+        }
+        cv_work.notify_all();
+        if (worker.joinable()) worker.join();
+        if (batch.stream) cudaStreamSynchronize(batch.stream);
+        for (auto& kv : reqs) {
+            kv.second.prep.reset();
+            if (kv.second.result) batch.pinned.release_now(kv.second.result);
+        }
+        for (TickRec& t : outstanding) recycle(t);
+        for (cudaEvent_t e : timing_events) cudaEventDestroy(e);
+        for (cudaEvent_t e : plain_events) cudaEventDestroy(e);
+        if (base_ev) cudaEventDestroy(base_ev);
+    }
+
+    cudaEvent_t take_event(bool timing)
+    {
+        std::vector<cudaEvent_t>& v = timing ? timing_events : plain_events;
+        if (!v.empty()) {
+            cudaEvent_t e = v.back();
+            v.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreateWithFlags(&e, timing ? cudaEventDefault : cudaEventDisableTiming);
+        return e;
+    }
+
+    void recycle(TickRec& t)
+    {
+        if (t.start) timing_events.push_back(t.start);
+        if (t.end) timing_events.push_back(t.end);
+        if (t.post) plain_events.push_back(t.post);
+        t.start = t.end = t.post = nullptr;
     }
 
     int submit(const dg_params& p, double dt, int steps, double t_arrival, long long* id)
@@ -70,24 +186,42 @@ struct Server {
             return fail(DG_ERR_NOMEM, "dg_serve_submit: request needs " + std::to_string(r.bytes) +
                                           " bytes, more than the whole HBM budget " + std::to_string(budget));
         r.t_arrival = t_arrival < 0.0 ? now() : t_arrival;
-        // keep pending sorted by arrival time
+        const double ta = r.t_arrival;
+        // keep pending and the preparation queue sorted by arrival time
         auto it = pending.begin();
-        while (it != pending.end() && reqs[*it].t_arrival <= r.t_arrival) ++it;
+        while (it != pending.end() && reqs[*it].t_arrival <= ta) ++it;
         pending.insert(it, r.id);
-        if (id) *id = r.id;
-        reqs[r.id] = std::move(r);
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            auto jt = to_prepare.begin();
+            while (jt != to_prepare.end() && reqs[*jt].t_arrival <= ta) ++jt;
+            to_prepare.insert(jt, r.id);
+            if (id) *id = r.id;
+            reqs[r.id] = std::move(r);
+        }
+        cv_work.notify_one();
         return DG_OK;
     }
 
-    // Admit arrived requests in arrival order while their memory fits.
+    // Admit arrived, prepared requests in arrival order while their memory
+    // fits; each admission is stream-ordered device work only.
     int admit(double t)
     {
         while (!pending.empty()) {
             Req& r = reqs[pending.front()];
             if (r.t_arrival > t) break;
             if (in_use + r.bytes > budget) break;  // FIFO: later requests wait behind it
+            std::unique_ptr<Batch::Prepared> pr;
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                if (!r.prep_done) break;
+                pr = std::move(r.prep);
+                prepared_ahead--;
+                if (r.prep_rc) return fail(r.prep_rc, r.prep_err);
+            }
+            cv_work.notify_one();
             int idx = -1;
-            int rc = batch.add(r.p, r.dt, r.steps, nullptr, nullptr, &idx);
+            int rc = batch.commit(*pr, &idx);
             if (rc) return rc;
             in_use += r.bytes;
             r.t_admit = now();
@@ -97,66 +231,141 @@ struct Server {
         return DG_OK;
     }
 
-    int retire(double t)
+    bool prepared(const Req& r)
     {
-        for (int i = (int)inflight.size() - 1; i >= 0; i--) {
-            Req& r = reqs[inflight[i]];
-            if (r.remaining > 0) continue;
-            if (keep_results) {
-                const Batch::Entry& E = batch.probs[i];
-                for (int a = 0; a < 3; a++) r.dims[a] = E.dims[a];
-                const size_t g = (size_t)E.dims[0] * E.dims[1] * E.dims[2];
-                r.rho.resize(g);
-                r.vel.resize(3 * g);
-                int rc = batch.get_state(i, r.rho.data(), r.vel.data());
-                if (rc) return rc;
-            }
-            r.t_done = t;
-            int rc = batch.remove(i);
-            if (rc) return rc;
-            in_use -= r.bytes;
-            inflight.erase(inflight.begin() + i);
-        }
-        return DG_OK;
+        std::lock_guard<std::mutex> lock(mu);
+        return r.prep_done;
     }
 
     // Steps the next tick may run without delaying a retirement or the
     // admission of the next arrival: up to the first in-flight solve's end,
     // and only as many steps as fit before the next pending arrival.
-    int steps_this_tick(double t) const
+    int steps_this_tick(double t)
     {
         int k = kMaxStepsPerTick;
         for (long long id : inflight) k = std::min(k, reqs.at(id).remaining);
         if (!pending.empty()) {
-            const double wait = reqs.at(pending.front()).t_arrival - t;
-            if (wait <= 0.0) return 1;  // arrived, waiting for memory: retire as soon as possible
-            if (step_s > 0.0) k = std::min(k, std::max(1, (int)(wait / step_s)));
-            else k = 1;
+            Req& f = reqs.at(pending.front());
+            const double wait = f.t_arrival - t;
+            if (wait <= 0.0) {
+                // arrived: waiting for memory (freed by the next retirement)
+                // or for its preparation (admit as soon as it is ready)
+                if (in_use + f.bytes <= budget) k = 1;
+            } else if (step_s > 0.0) {
+                k = std::min(k, std::max(1, (int)(wait / step_s)));
+            } else {
+                k = 1;
+            }
         }
         return std::max(1, k);
     }
 
-    // One iteration: admit, advance every in-flight solve by the tick's
-    // steps (one graph replay each, one host synchronisation), retire.
+    // Completion of an enqueued tick: stamps its retired requests with the
+    // device time their last step ended (on the host clock) and collects
+    // their results.
+    int finish(TickRec& t, bool block, bool* done)
+    {
+        cudaError_t e = block ? cudaEventSynchronize(t.post) : cudaEventQuery(t.post);
+        if (e == cudaErrorNotReady) {
+            (void)cudaGetLastError();
+            *done = false;
+            return DG_OK;
+        }
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("serve: ") + cudaGetErrorString(e));
+        *done = true;
+        float ms_end = 0.f, ms_run = 0.f;
+        e = cudaEventElapsedTime(&ms_end, base_ev, t.end);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms_run, t.start, t.end);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventElapsedTime: ") + cudaGetErrorString(e));
+        const double t_end = t_base + ms_end * 1e-3;
+        busy_s += ms_run * 1e-3;
+        const double per = ms_run * 1e-3 / t.k;
+        step_s = step_s > 0.0 ? 0.8 * step_s + 0.2 * per : per;
+        for (long long id : t.done) {
+            Req& r = reqs[id];
+            r.t_done = t_end;
+            if (r.result) {
+                const size_t g = (size_t)r.dims[0] * r.dims[1] * r.dims[2];
+                const double* src = (const double*)r.result->ptr;
+                r.rho.assign(src, src + g);
+                r.vel.assign(src + g, src + 4 * g);
+                batch.pinned.release_now(r.result);
+                r.result = nullptr;
+            }
+        }
+        recycle(t);
+        return DG_OK;
+    }
+
+    int collect(bool block_all)
+    {
+        while (!outstanding.empty()) {
+            bool done = false;
+            int rc = finish(outstanding.front(), block_all || (int)outstanding.size() > kDepth, &done);
+            if (rc) return rc;
+            if (!done) break;
+            outstanding.pop_front();
+        }
+        return DG_OK;
+    }
+
+    // One iteration: collect finished ticks, admit, enqueue the tick's steps
+    // for every in-flight solve (one graph replay each) and the retirement of
+    // the solves they complete (result copy, memory back to the pool), with no
+    // host synchronisation; the host waits only to stay at most kDepth ticks
+    // ahead of the device, or to drain when nothing is in flight.
     int tick(int* n_inflight)
     {
-        int rc = admit(now());
+        int rc = collect(false);
+        if (rc) return rc;
+        rc = admit(now());
         if (rc) return rc;
         if (!inflight.empty()) {
-            const double t_start = now();
-            const int k = steps_this_tick(t_start);
+            const int k = steps_this_tick(now());
+            TickRec t;
+            t.k = k;
+            t.start = take_event(true);
+            t.end = take_event(true);
+            t.post = take_event(false);
+            cudaStream_t st = batch.stream;
+            cudaError_t e = cudaEventRecord(t.start, st);
+            if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
             rc = batch.step(k);
             if (rc) return rc;
-            cudaError_t e = cudaStreamSynchronize(batch.stream);
-            if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
-            const double per = (now() - t_start) / k;
-            step_s = step_s > 0.0 ? 0.8 * step_s + 0.2 * per : per;
-            for (long long id : inflight) reqs[id].remaining -= k;
+            e = cudaEventRecord(t.end, st);
+            if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+            for (size_t i = 0; i < inflight.size(); i++) {
+                const Batch::Entry& E = batch.probs[i];
+                work += 4.0 * E.n_elem * E.K * E.K * E.K * 3.0 * k;
+                reqs[inflight[i]].remaining -= k;
+            }
             ticks += k;
             inflight_sum += (double)inflight.size() * k;
-            rc = retire(now());
-            if (rc) return rc;
+            for (int i = (int)inflight.size() - 1; i >= 0; i--) {
+                Req& r = reqs[inflight[i]];
+                if (r.remaining > 0) continue;
+                const Batch::Entry& E = batch.probs[i];
+                for (int a = 0; a < 3; a++) r.dims[a] = E.dims[a];
+                if (keep_results) {
+                    const size_t g = (size_t)E.dims[0] * E.dims[1] * E.dims[2];
+                    std::string err;
+                    r.result = batch.pinned.acquire(4 * g * sizeof(double), err);
+                    if (!r.result) return fail(DG_ERR_CUDA, "serve: " + err);
+                    rc = batch.enqueue_state_copy(i, r.steps, r.result);
+                    if (rc) return rc;
+                }
+                rc = batch.remove(i);
+                if (rc) return rc;
+                in_use -= r.bytes;
+                t.done.push_back(r.id);
+                inflight.erase(inflight.begin() + i);
+            }
+            e = cudaEventRecord(t.post, st);
+            if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+            outstanding.push_back(std::move(t));
         }
+        rc = collect(inflight.empty());
+        if (rc) return rc;
         if (n_inflight) *n_inflight = (int)inflight.size();
         return DG_OK;
     }
@@ -164,11 +373,17 @@ struct Server {
     int run(double max_seconds)
     {
         const double t_end = now() + (max_seconds > 0 ? max_seconds : 1e300);
-        while (!pending.empty() || !inflight.empty()) {
+        while (!pending.empty() || !inflight.empty() || !outstanding.empty()) {
             if (now() > t_end) return fail(DG_ERR_STATE, "dg_serve_run: time limit reached");
             if (inflight.empty() && !pending.empty()) {
-                const double wait = reqs[pending.front()].t_arrival - now();
-                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+                Req& f = reqs[pending.front()];
+                const double wait = f.t_arrival - now();
+                if (wait > 0) {
+                    std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+                } else if (!prepared(f)) {
+                    std::unique_lock<std::mutex> lock(mu);
+                    cv_ready.wait_for(lock, std::chrono::milliseconds(1), [&] { return f.prep_done; });
+                }
             }
             int n = 0;
             int rc = tick(&n);
@@ -192,9 +407,7 @@ int dg_serve_create(size_t hbm_budget_bytes, int keep_results, dg_server** out)
     *out = nullptr;
     dg_server* h = new (std::nothrow) dg_server;
     if (!h) return dg::fail(DG_ERR_NOMEM, "dg_serve_create: host allocation failed");
-    h->s.budget = hbm_budget_bytes;
-    h->s.keep_results = keep_results != 0;
-    int rc = h->s.batch.init(64);
+    int rc = h->s.init(hbm_budget_bytes, keep_results != 0);
     if (rc) {
         delete h;
         return rc;
@@ -273,6 +486,22 @@ int dg_serve_stats(dg_server* s, int* completed, double* p50, double* p99, doubl
     if (p99) *p99 = pct(0.99);
     if (solves_per_s) *solves_per_s = lat.empty() ? 0.0 : lat.size() / std::max(1e-9, last - first);
     if (mean_inflight) *mean_inflight = s->s.ticks ? s->s.inflight_sum / s->s.ticks : 0.0;
+    return DG_OK;
+}
+
+int dg_serve_utilization(dg_server* s, double* gpu_busy_s, double* span_s, double* dof_stage_updates)
+{
+    if (!s) return dg::fail(DG_ERR_INVALID, "dg_serve_utilization: null handle");
+    double first = 1e300, last = 0.0;
+    for (const auto& kv : s->s.reqs) {
+        const dg::Server::Req& r = kv.second;
+        if (r.t_done < 0.0) continue;
+        first = std::min(first, r.t_arrival);
+        last = std::max(last, r.t_done);
+    }
+    if (gpu_busy_s) *gpu_busy_s = s->s.busy_s;
+    if (span_s) *span_s = last > first ? last - first : 0.0;
+    if (dof_stage_updates) *dof_stage_updates = s->s.work;
     return DG_OK;
 }
 

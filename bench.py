@@ -55,9 +55,12 @@ def args_():
                     help="problems of the batched form (config 4 has 256; fewer only for profiling)")
     ap.add_argument("--batch-tune-steps", type=int, default=2,
                     help="RK steps per autotuner trial (0: no autotuning, default tiles)")
-    ap.add_argument("--serve-requests", type=int, default=24, help="requests per arrival rate (serving form)")
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[5.0, 20.0, 50.0, 200.0])
-    ap.add_argument("--serve-baseline-rates", type=float, nargs="*", default=[5.0, 200.0])
+    ap.add_argument("--serve-requests", type=int, default=500, help="requests per arrival rate (serving form)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[15.0, 30.0, 100.0],
+                    help="arrival rates (solves/s): one below and one above the server's capacity")
+    ap.add_argument("--serve-baseline-rates", type=float, nargs="*", default=[15.0, 100.0])
+    ap.add_argument("--serve-baseline-requests", type=int, default=24,
+                    help="first requests of a trace served one at a time through the FP64 plain path")
     return ap.parse_args()
 
 
@@ -553,19 +556,28 @@ def serving_form(a, dg, W):
             t0 = srv.clock + 0.05
             for c, ta in zip(cfgs, arr):
                 srv.submit(c, arrival_time=t0 + ta)
-            srv.run(max_seconds=600)
+            srv.run(max_seconds=900)
             st = srv.stats()
+            u = srv.utilization()
         work = sum(W.dof_count(c) * 3 * c["STEPS"] for c in cfgs)
-        row = {"rate_per_s": rate, "p50_s": st["p50_s"], "p99_s": st["p99_s"], "solves_per_s": st["solves_per_s"],
-               "mean_inflight": st["mean_inflight"], "completed": st["completed"],
-               "dof_stage_updates": work,
+        row = {"rate_per_s": rate, "requests": len(cfgs),
+               # the seeded Poisson trace's own rate: (n - 1) / (last arrival - first arrival)
+               "arrival_rate_realized": (len(arr) - 1) / max(1e-9, arr[-1] - arr[0]),
+               "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+               "solves_per_s": st["solves_per_s"], "mean_inflight": st["mean_inflight"],
+               "completed": st["completed"], "dof_stage_updates": work,
                # served throughput over the trace's span (first arrival to last completion)
-               "dof_stage_updates_per_s": work * st["solves_per_s"] / max(1, st["completed"])}
+               "dof_stage_updates_per_s": work / max(1e-9, u["span_s"]),
+               # device time inside RK steps over the span, and the throughput over that time
+               "gpu_busy_frac": u["busy_frac"],
+               "dof_stage_updates_per_gpu_busy_s": u["dof_stage_updates"] / max(1e-9, u["gpu_busy_s"])}
         row["hbm_frac"] = hbm_roofline(row["dof_stage_updates_per_s"])["frac"]
         if rate in a.serve_baseline_rates:
+            nb = min(len(cfgs), a.serve_baseline_requests)
+            bwork = sum(W.dof_count(c) * 3 * c["STEPS"] for c in cfgs[:nb])
             lat, span0, span1, prev_done = [], None, 0.0, 0.0
             start = time.perf_counter()
-            for c, ta in zip(cfgs, arr):
+            for c, ta in zip(cfgs[:nb], arr[:nb]):
                 c64 = dict(c)
                 c64["PRECISION"] = 64
                 begin = max(ta, prev_done)
@@ -579,8 +591,9 @@ def serving_form(a, dg, W):
                 lat.append(prev_done - ta)
             lat.sort()
             span = max(1e-9, prev_done - arr[0])
-            row["fp64_one_at_a_time"] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                                         "solves_per_s": len(lat) / span, "dof_stage_updates_per_s": work / span}
+            row["fp64_one_at_a_time"] = {"requests": nb, "p50_s": float(np.percentile(lat, 50)),
+                                         "p99_s": float(np.percentile(lat, 99)),
+                                         "solves_per_s": len(lat) / span, "dof_stage_updates_per_s": bwork / span}
         out["rates"].append(row)
     # error of served results against the FP64 plain path: one request per order of the first
     # trace, served together (untimed, results kept) and each solved alone in FP64
@@ -651,6 +664,14 @@ def main():
                     top = max(sf["rates"], key=lambda r: r["rate_per_s"])
                     sf["saturated_dof_stage_updates_per_s"] = top["dof_stage_updates_per_s"]
                     sf["saturated_vs_fp64_plain"] = top["dof_stage_updates_per_s"] / line["value"]
+                    sf["capacity_solves_per_s"] = top["solves_per_s"]
+                    # highest tested rate the server keeps up with (completions keep pace with arrivals)
+                    kept = [r["rate_per_s"] for r in sf["rates"]
+                            if r["solves_per_s"] >= 0.95 * r["arrival_rate_realized"]]
+                    sf["sustained_rate_per_s"] = max(kept) if kept else None
+                    if bf:
+                        sf["saturated_busy_vs_batched"] = top["dof_stage_updates_per_gpu_busy_s"] / bf["value"]
+                        sf["saturated_span_vs_batched"] = top["dof_stage_updates_per_s"] / bf["value"]
         if line is not None:
             print(json.dumps(line), flush=True)
     finally:

@@ -304,12 +304,19 @@ double dg_serve_clock(const dg_server* s);
  * with DG_ERR_NOMEM if it alone exceeds the budget. */
 int dg_serve_submit(dg_server* s, const dg_params* p, double dt, int steps, double arrival_time,
                     long long* id);
-/* One loop iteration: admit arrived requests that fit, advance every in-flight
- * solve by the same number of RK steps (one graph replay each, then one host
- * synchronisation): as many as end no in-flight solve early and, while a
- * request is still to arrive, as fit before its arrival by the running
- * estimate of a step's time (at most 64; one while an arrived request waits
- * for memory); then retire the finished ones. */
+/* One loop iteration: collect the ticks the device has finished (their
+ * requests get their completion times and results), admit arrived requests
+ * that fit and whose host preparation (mesh tables, operators, staged in
+ * page-locked memory by the server's worker thread) is done, enqueue for every
+ * in-flight solve the same number of RK steps (one graph replay each): as many
+ * as end no in-flight solve early and, while a request is still to arrive, as
+ * fit before its arrival by the running estimate of a step's time (at most
+ * 64; one while an arrived request waits for its preparation), and enqueue
+ * the retirement of the solves these steps complete (result copy, memory back
+ * to the server's device memory pool).  Admission and retirement are
+ * stream-ordered device work, so the host never synchronises the device for
+ * them; it waits only to stay at most two ticks ahead of the device, and
+ * drains when nothing is in flight.  Call submit and tick from one thread. */
 int dg_serve_tick(dg_server* s, int* n_inflight);
 /* Run the loop in real time until every submitted request has finished. */
 int dg_serve_run(dg_server* s, double max_seconds);
@@ -321,6 +328,11 @@ int dg_serve_result(dg_server* s, long long id, double* t_arrival, double* t_adm
  * the span from the first arrival to the last completion, mean in-flight count. */
 int dg_serve_stats(dg_server* s, int* completed, double* p50, double* p99, double* solves_per_s,
                    double* mean_inflight);
+/* Device time spent in RK steps (CUDA events around each tick's steps), the
+ * span from the first arrival to the last completion, and the DOF-stage
+ * updates performed (4 fields x nodes x 3 stages x steps, summed over every
+ * solve); busy / span is the device's busy fraction over the trace. */
+int dg_serve_utilization(dg_server* s, double* gpu_busy_s, double* span_s, double* dof_stage_updates);
 
 /* Last error message of this thread ("" if none). */
 const char* dg_last_error(void);

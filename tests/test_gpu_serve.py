@@ -29,8 +29,10 @@ def test_results_same_alone_and_in_the_mix():
     m = dg()
     cfgs = requests()
     with m.Server(hbm_budget_bytes=8 << 30, keep_results=True) as srv:
+        # all arrive together; the first is admitted as soon as its host
+        # preparation is done, the others join it while it runs
         t0 = srv.clock
-        ids = [srv.submit(c, arrival_time=t0 + 0.002 * k) for k, c in enumerate(cfgs)]
+        ids = [srv.submit(c, arrival_time=t0) for c in cfgs]
         srv.run(max_seconds=120)
         res = [srv.result(i, state=True) for i in ids]
         st = srv.stats()
@@ -49,7 +51,7 @@ def test_admission_respects_the_hbm_budget():
     for c in cfgs:
         c["NUM_ELEMENTS"] = [6, 6, 6]
         c["ORDER"] = 3
-        c["STEPS"] = 15
+        c["STEPS"] = 300  # long enough that the next request is prepared while one runs
     per = 216 * 64 * 23 * 4 + 216 * 28
     with m.Server(hbm_budget_bytes=2 * per + 100) as srv:
         for c in cfgs:
@@ -70,3 +72,31 @@ def test_request_larger_than_budget_rejected():
     with m.Server(hbm_budget_bytes=1 << 20) as srv:
         with pytest.raises(m.DGError, match="more than the whole HBM budget"):
             srv.submit(c)
+
+
+def test_steady_stream_accounting():
+    """A stream of requests arriving while others run: every request completes
+    after it arrived and was admitted, the device-busy time is positive and
+    at most the span, and the DOF-stage updates the server counts equal the
+    requests' own (4 fields x nodes x 3 stages x steps)."""
+    m = dg()
+    W = workloads()
+    cfgs = requests(n=40, seed=9)
+    rng = np.random.default_rng(9)
+    with m.Server(hbm_budget_bytes=4 << 30) as srv:
+        t0 = srv.clock + 0.01
+        t, ids = t0, []
+        for c in cfgs:
+            t += float(rng.exponential(0.004))
+            ids.append(srv.submit(c, arrival_time=t))
+        srv.run(max_seconds=120)
+        st = srv.stats()
+        u = srv.utilization()
+        res = [srv.result(i) for i in ids]
+    assert st["completed"] == len(cfgs)
+    for r in res:
+        assert r["done"] >= r["admit"] >= r["arrival"]
+    want = sum(W.dof_count(c) * 3 * c["STEPS"] for c in cfgs)
+    assert abs(u["dof_stage_updates"] - want) <= 1e-9 * want
+    assert 0.0 < u["gpu_busy_s"] <= u["span_s"] * 1.001
+    assert st["p99_s"] >= st["p50_s"] > 0.0
