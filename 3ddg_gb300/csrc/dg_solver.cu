@@ -469,6 +469,8 @@ int Solver::step(double dt, int nsteps)
     }
     for (int n = 0; n < nsteps; n++) {
         for (int s = 0; s < 3; s++) {
+            // stage 3 writes U in place (FP64) or the other u buffer (FP32)
+            if (s == 2) wait_pack(stream, fp64() ? buf[0] : buf[1 - cur]);
             int rc = fp64() ? rk_stage_fp64(s, dt, nullptr) : rk_stage_fp32(s, dt, nullptr);
             if (rc) return rc;
         }
@@ -553,6 +555,7 @@ int Solver::pack_out(const void* src, double* drho, double* vel)
 
 int Solver::unpack_in(const double* drho, const double* vel)
 {
+    wait_pack(stream, state_ptr());
     const double* rho_d = (const double*)device_view(drho);
     const double* vel_d = (const double*)device_view(vel);
     const bool staged = !rho_d || !vel_d;
@@ -570,8 +573,29 @@ int Solver::unpack_in(const double* drho, const double* vel)
     return DG_OK;
 }
 
-// Host-order arrays -> state on the compute stream: device staging is walked in
-// element order, pinned host memory (read over the CPU-GPU link) in host order.
+template <typename T>
+cudaError_t Solver::launch_unpack_tiled(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
+                                        const FluxOut<T>& fo, cudaStream_t st)
+{
+    const size_t fs = mesh.fstride();
+    const int nb = mesh.nb[0] * mesh.nb[1] * mesh.nb[2];
+    auto grid = [&](int cz) { return (unsigned)(nb * mesh.ne[0] * mesh.ne[1] * ((mesh.ne[2] + cz - 1) / cz)); };
+    switch (mesh.K) {
+    case 2: unpack_tiled_kernel<T, 2><<<grid(unpack_cz<2>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 3: unpack_tiled_kernel<T, 3><<<grid(unpack_cz<3>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 4: unpack_tiled_kernel<T, 4><<<grid(unpack_cz<4>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 5: unpack_tiled_kernel<T, 5><<<grid(unpack_cz<5>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 6: unpack_tiled_kernel<T, 6><<<grid(unpack_cz<6>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 7: unpack_tiled_kernel<T, 7><<<grid(unpack_cz<7>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    case 8: unpack_tiled_kernel<T, 8><<<grid(unpack_cz<8>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Host-order arrays -> state on the compute stream: device staging by the
+// tiled transpose, pinned host memory (read over the CPU-GPU link) in host
+// order.
 int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_device)
 {
     const GridMap g = grid_map(mesh);
@@ -581,12 +605,9 @@ int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_devi
     const FluxOut<double> fo = flux_consts<double>(d_flux[flux_cur], p.rho0, p.c0, p.b_over_a);
     const FluxOut<float> none = flux_consts<float>(nullptr, p.rho0, p.c0, p.b_over_a);
     if (on_device) {
-        if (fp64())
-            unpack_elem_order_kernel<double><<<blocks, 256, 0, stream>>>((double*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                         g, mesh.n_elem, rho_d, vel_d, gsize(), fo);
-        else
-            unpack_elem_order_kernel<float><<<blocks, 256, 0, stream>>>((float*)state_ptr(), mesh.fstride(), mesh.NP,
-                                                                        g, mesh.n_elem, rho_d, vel_d, gsize(), none);
+        cudaError_t e = fp64() ? launch_unpack_tiled<double>((double*)state_ptr(), g, rho_d, vel_d, fo, stream)
+                               : launch_unpack_tiled<float>((float*)state_ptr(), g, rho_d, vel_d, none, stream);
+        if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("unpack: ") + cudaGetErrorString(e));
     } else {
         if (fp64())
             unpack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((double*)state_ptr(), mesh.fstride(),
@@ -603,11 +624,30 @@ int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_devi
     return DG_OK;
 }
 
+void Solver::wait_pack(cudaStream_t st, const void* target)
+{
+    for (const PackEvent& pe : pack_ev)
+        if (pe.ev && pe.src == target) cudaStreamWaitEvent(st, pe.ev, 0);
+}
+
 int Solver::ensure_async()
 {
     // Each resource is created once; a call after a failed one resumes here.
     if (!copy_in) DG_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
     if (!copy_out) DG_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    if (!xin || !xout) {
+        int lo = 0, hi = 0;
+        DG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        if (!xin) DG_CUDA(cudaStreamCreateWithPriority(&xin, cudaStreamNonBlocking, hi));
+        if (!xout) DG_CUDA(cudaStreamCreateWithPriority(&xout, cudaStreamNonBlocking, hi));
+    }
+    const size_t es = fp64() ? sizeof(double) : sizeof(float);
+    if (!spare_u) DG_CUDA(cudaMalloc(&spare_u, 4 * mesh.fstride() * es));
+    if (fp64() && d_flux[0] && !spare_f) DG_CUDA(cudaMalloc(&spare_f, 4 * mesh.fstride() * sizeof(double)));
+    for (cudaEvent_t* e : {&spare_ready, &spare_free, &step_done})
+        if (!*e) DG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (PackEvent& pe : pack_ev)
+        if (!pe.ev) DG_CUDA(cudaEventCreateWithFlags(&pe.ev, cudaEventDisableTiming));
     for (int i = 0; i < 2; i++) {
         if (!astage_in[i]) DG_CUDA(cudaMalloc(&astage_in[i], 4 * gsize() * sizeof(double)));
         if (!astage_out[i]) DG_CUDA(cudaMalloc(&astage_out[i], 4 * gsize() * sizeof(double)));
@@ -617,8 +657,11 @@ int Solver::ensure_async()
     return DG_OK;
 }
 
-// Upload on the copy-in stream into staging slot k, then unpack on the compute
-// stream.  The slot is reused only after the unpack that last read it.
+// Upload on the copy-in stream into staging slot k; unpack on the xin stream
+// into the spare state (and flux) buffer once the steps and the pack that
+// last used it are done, so it runs under the step enqueued before; the
+// compute stream swaps it in at this point of the call sequence.  The slot is
+// reused only after the unpack that last read it.
 int Solver::set_state_async(const double* drho, const double* vel)
 {
     if (!device_view(drho) || !device_view(vel))
@@ -633,15 +676,40 @@ int Solver::set_state_async(const double* drho, const double* vel)
     DG_CUDA(cudaMemcpyAsync(st, drho, n * sizeof(double), cudaMemcpyHostToDevice, copy_in));
     DG_CUDA(cudaMemcpyAsync(st + n, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, copy_in));
     DG_CUDA(cudaEventRecord(in_ready[k], copy_in));
-    DG_CUDA(cudaStreamWaitEvent(stream, in_ready[k], 0));
-    rc = launch_unpack(st, st + n, true);
-    if (rc) return rc;
-    DG_CUDA(cudaEventRecord(in_free[k], stream));
+    DG_CUDA(cudaStreamWaitEvent(xin, in_ready[k], 0));
+    if (spare_free_recorded) DG_CUDA(cudaStreamWaitEvent(xin, spare_free, 0));
+    wait_pack(xin, spare_u);
+    const GridMap g = grid_map(mesh);
+    cudaError_t e;
+    if (fp64()) {
+        const FluxOut<double> fo = flux_consts<double>(spare_f, p.rho0, p.c0, p.b_over_a);
+        e = launch_unpack_tiled<double>((double*)spare_u, g, st, st + n, fo, xin);
+    } else {
+        const FluxOut<float> none = flux_consts<float>(nullptr, p.rho0, p.c0, p.b_over_a);
+        e = launch_unpack_tiled<float>((float*)spare_u, g, st, st + n, none, xin);
+    }
+    if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("unpack: ") + cudaGetErrorString(e));
+    launches++;
+    DG_CUDA(cudaEventRecord(in_free[k], xin));
+    DG_CUDA(cudaEventRecord(spare_ready, xin));
+    // swap the uploaded state (and its fluxes) in on the compute stream
+    DG_CUDA(cudaStreamWaitEvent(stream, spare_ready, 0));
+    void*& cur_u = fp64() ? buf[0] : buf[cur];
+    std::swap(cur_u, spare_u);
+    if (spare_f) std::swap(d_flux[flux_cur], spare_f);
+    if (!fp64()) DG_CUDA(cudaMemsetAsync(buf[2], 0, 4 * mesh.fstride() * sizeof(float), stream));  // Kahan compensation
+    flux_valid = fp64() && d_flux[0] != nullptr;
+    ic_live = false;
+    // the buffers swapped out are free once the work enqueued so far is done
+    DG_CUDA(cudaEventRecord(spare_free, stream));
+    spare_free_recorded = true;
     return DG_OK;
 }
 
-// Pack on the compute stream into staging slot k (after the download that last
-// read the slot), then download on the copy-out stream.
+// Pack on the xout stream into staging slot k (after the steps enqueued so
+// far and the download that last read the slot), then download on the
+// copy-out stream.  The compute stream goes on with the next steps and waits
+// for this pack only before it writes the state buffer the pack reads.
 int Solver::get_state_async(double* drho, double* vel)
 {
     if ((drho && !device_view(drho)) || (vel && !device_view(vel)))
@@ -652,20 +720,31 @@ int Solver::get_state_async(double* drho, double* vel)
     out_slot ^= 1;
     const size_t n = gsize();
     double* st = astage_out[k];
-    DG_CUDA(cudaStreamWaitEvent(stream, out_free[k], 0));
+    DG_CUDA(cudaEventRecord(step_done, stream));
+    DG_CUDA(cudaStreamWaitEvent(xout, step_done, 0));
+    DG_CUDA(cudaStreamWaitEvent(xout, out_free[k], 0));
     const GridMap g = grid_map(mesh);
     const int threads = 128, blocks = 152 * 16;
     if (fp64())
-        pack_host_order_kernel<double><<<blocks, threads, 0, stream>>>((const double*)state_ptr(), mesh.fstride(),
-                                                                       mesh.NP, g, drho ? st : nullptr,
-                                                                       vel ? st + n : nullptr, n);
+        pack_host_order_kernel<double><<<blocks, threads, 0, xout>>>((const double*)state_ptr(), mesh.fstride(),
+                                                                     mesh.NP, g, drho ? st : nullptr,
+                                                                     vel ? st + n : nullptr, n);
     else
-        pack_host_order_kernel<float><<<blocks, threads, 0, stream>>>((const float*)state_ptr(), mesh.fstride(),
-                                                                      mesh.NP, g, drho ? st : nullptr,
-                                                                      vel ? st + n : nullptr, n);
+        pack_host_order_kernel<float><<<blocks, threads, 0, xout>>>((const float*)state_ptr(), mesh.fstride(),
+                                                                    mesh.NP, g, drho ? st : nullptr,
+                                                                    vel ? st + n : nullptr, n);
     launches++;
     DG_CUDA(cudaGetLastError());
-    DG_CUDA(cudaEventRecord(out_ready[k], stream));
+    DG_CUDA(cudaEventRecord(out_ready[k], xout));
+    // one event per state buffer: the pack of this buffer is done
+    PackEvent* pe = nullptr;
+    for (PackEvent& x : pack_ev)
+        if (x.src == state_ptr()) pe = &x;
+    for (PackEvent& x : pack_ev)
+        if (!pe && !x.src) pe = &x;
+    if (!pe) return fail(DG_ERR_STATE, "dg_get_state_async: more state buffers than pack events");
+    pe->src = state_ptr();
+    DG_CUDA(cudaEventRecord(pe->ev, xout));
     DG_CUDA(cudaStreamWaitEvent(copy_out, out_ready[k], 0));
     if (drho) DG_CUDA(cudaMemcpyAsync(drho, st, n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
     if (vel) DG_CUDA(cudaMemcpyAsync(vel, st + n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
@@ -676,6 +755,8 @@ int Solver::get_state_async(double* drho, double* vel)
 int Solver::sync_all()
 {
     DG_CUDA(cudaStreamSynchronize(stream));
+    if (xin) DG_CUDA(cudaStreamSynchronize(xin));
+    if (xout) DG_CUDA(cudaStreamSynchronize(xout));
     if (copy_in) DG_CUDA(cudaStreamSynchronize(copy_in));
     if (copy_out) DG_CUDA(cudaStreamSynchronize(copy_out));
     return DG_OK;
@@ -804,7 +885,7 @@ void Solver::prof_reset()
 Solver::~Solver()
 {
     if (stream) cudaStreamSynchronize(stream);
-    for (cudaStream_t c : {copy_in, copy_out})
+    for (cudaStream_t c : {xin, xout, copy_in, copy_out})
         if (c) {
             cudaStreamSynchronize(c);
             cudaStreamDestroy(c);
@@ -815,6 +896,12 @@ Solver::~Solver()
         for (cudaEvent_t e : {in_ready[i], in_free[i], out_ready[i], out_free[i]})
             if (e) cudaEventDestroy(e);
     }
+    for (cudaEvent_t e : {spare_ready, spare_free, step_done})
+        if (e) cudaEventDestroy(e);
+    for (PackEvent& pe : pack_ev)
+        if (pe.ev) cudaEventDestroy(pe.ev);
+    if (spare_u) cudaFree(spare_u);
+    if (spare_f) cudaFree(spare_f);
     prof_reset();
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
     for (void* b : buf)
@@ -1047,6 +1134,7 @@ int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_ele
     // the caller may write the state: the next FP64 stage evaluates the volume
     // fluxes from it instead of reading the ones cached by the last stage
     h->s.flux_valid = false;
+    h->s.wait_pack(h->s.stream, h->s.state_ptr());
     const size_t es = h->s.fp64() ? 8 : 4;
     char* b = (char*)h->s.state_ptr();
     for (int f = 0; f < 4; f++) base[f] = b + (size_t)f * h->s.mesh.fstride() * es;

@@ -14,6 +14,10 @@
 
 namespace dg {
 
+struct GridMap;
+template <typename T>
+struct FluxOut;
+
 extern thread_local std::string g_last_error;
 int fail(int code, const std::string& msg);
 double burst_pressure(const dg_params& p, double t);
@@ -89,10 +93,32 @@ struct Solver {
     int pack_out(const void* src, double* drho, double* vel);
     int unpack_in(const double* drho, const double* vel);
     int launch_unpack(const double* rho_d, const double* vel_d, bool on_device);
+    template <typename T>
+    cudaError_t launch_unpack_tiled(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
+                                    const FluxOut<T>& fo, cudaStream_t st);
 
     // Asynchronous host transfers (dg_set_state_async / dg_get_state_async):
     // copy-engine streams and double-buffered device staging, so that one
-    // step's upload and the previous step's download run under compute.
+    // step's upload and the previous step's download run under compute.  The
+    // transposes between staging and the element-major state run on two
+    // high-priority streams of their own: an upload is unpacked (xin) into a
+    // spare state buffer (and, FP64 with advection, a spare flux buffer) that
+    // the compute stream swaps in at the upload's place in the call sequence,
+    // so the unpack runs under the step before; a download's pack (xout)
+    // reads the state while the next steps compute.  A stream waits for a
+    // pending pack only before it writes the buffer that pack reads (one
+    // completion event per state buffer).
+    cudaStream_t xin = nullptr, xout = nullptr;
+    void* spare_u = nullptr;
+    double* spare_f = nullptr;
+    cudaEvent_t spare_ready = nullptr, spare_free = nullptr, step_done = nullptr;
+    bool spare_free_recorded = false;
+    struct PackEvent {
+        const void* src = nullptr;
+        cudaEvent_t ev = nullptr;
+    };
+    PackEvent pack_ev[3];  // FP32 has three state buffers (u ping-pong and the spare)
+    void wait_pack(cudaStream_t st, const void* target);
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     double* astage_in[2] = {nullptr, nullptr};
     double* astage_out[2] = {nullptr, nullptr};

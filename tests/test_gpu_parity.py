@@ -466,3 +466,76 @@ def test_tiny_meshes_match_oracle(ne, periodic, order, solver_for, oracle_for):
     r32, _ = s32.state()
     p64, p32 = pressure(cfg, r64), pressure(cfg, r32)
     assert np.linalg.norm(p32 - p64) <= 1e-5 * np.linalg.norm(p64)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("order,ne,nb", [(1, (2, 3, 19), (1, 1, 1)), (2, (3, 2, 17), (2, 1, 2)),
+                                         (3, (2, 2, 9), (1, 2, 2)), (4, (3, 2, 18), (2, 2, 1)),
+                                         (5, (2, 3, 9), (1, 1, 2)), (6, (2, 2, 5), (2, 1, 1)),
+                                         (7, (2, 1, 5), (1, 1, 2))])
+def test_set_state_round_trip_every_order(order, ne, nb, precision, solver_for):
+    """dg_set_state from pageable memory goes through device staging and the
+    tiled transpose into the element-major state (z runs of 4, 8 or 16
+    elements per CTA, ragged at the end of a block row); reading it back gives
+    the same values (FP64: bitwise; FP32: the values rounded to float)."""
+    cfg = small(order=order, ne=ne)
+    cfg["NUM_BLOCKS"] = list(nb)
+    cfg["PRECISION"] = precision
+    s = solver_for(cfg)
+    X, Y, Z = s.dims
+    rng = np.random.default_rng(order)
+    r = rng.standard_normal((X, Y, Z))
+    v = rng.standard_normal((3, X, Y, Z))
+    s.set_state(r, v)
+    r2, v2 = s.state()
+    if precision == 64:
+        assert np.array_equal(r2, r) and np.array_equal(v2, v)
+    else:
+        assert np.array_equal(r2, r.astype(np.float32).astype(np.float64))
+        assert np.array_equal(v2, v.astype(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("precision,advect", [(64, 1), (64, 0), (32, 1)])
+def test_async_uploads_back_to_back(precision, advect, solver_for):
+    """Asynchronous uploads land in a spare state buffer that is swapped in at
+    their place in the call sequence: two uploads in a row (the second reuses
+    the buffer the first swapped out), a step, a download, then an upload
+    followed at once by a download, give what the synchronous calls give.
+    With advection off there are no volume-flux buffers to swap."""
+    import torch
+    cfg = small(order=3, ne=(2, 3, 3))
+    cfg["PRECISION"] = precision
+    cfg["EVALUATE_ADVECTION"] = advect
+    a, b = solver_for(cfg), solver_for(cfg)
+    shape = a.dims
+    rng = np.random.default_rng(3)
+
+    def pinned(shp):
+        return torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
+
+    A = (pinned(shape), pinned((3,) + shape))
+    B = (pinned(shape), pinned((3,) + shape))
+    for r, v in (A, B):
+        r[...] = rng.standard_normal(shape) * 1e-3
+        v[...] = rng.standard_normal((3,) + shape) * 1e-6
+    out1 = (pinned(shape), pinned((3,) + shape))
+    out2 = (pinned(shape), pinned((3,) + shape))
+    a.set_state_async(*A)
+    a.set_state_async(*B)
+    a.step(cfg["DT"], 2)
+    a.state_async(*out1)
+    a.set_state_async(*A)
+    a.state_async(*out2)
+    a.step(cfg["DT"], 1)
+    a.synchronize()
+    b.set_state(*B)
+    b.step(cfg["DT"], 2)
+    r1, v1 = b.state()
+    assert np.array_equal(out1[0], r1) and np.array_equal(out1[1], v1)
+    b.set_state(*A)
+    r2, v2 = b.state()
+    assert np.array_equal(out2[0], r2) and np.array_equal(out2[1], v2)
+    b.step(cfg["DT"], 1)
+    ra, va = a.state()
+    rb, vb = b.state()
+    assert np.array_equal(ra, rb) and np.array_equal(va, vb)
