@@ -50,6 +50,8 @@ def args_():
     ap.add_argument("--elements", type=int, default=0,
                     help="profiling cases only: the config2 physics on E^3 elements in one block")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--order", type=int, default=0,
+                    help="polynomial order of the device-timed workload (default: config 2's N = 4)")
     ap.add_argument("--batch-steps", type=int, default=20, help="timed RK steps of the batched form")
     ap.add_argument("--batch-instances", type=int, default=256,
                     help="problems of the batched form (config 4 has 256; fewer only for profiling)")
@@ -296,6 +298,9 @@ def run_ours(a, dist: Dist):
     cfg = W.config2(seed=dist.rank)
     if a.elements:
         cfg = W.scaled(cfg, (a.elements,) * 3)
+    if a.order:
+        cfg["ORDER"] = a.order
+        cfg["DT"] = W.cfl_dt(cfg)
     if a.precision == 32:
         cfg["PRECISION"] = 32
     dt = cfg["DT"]
@@ -385,14 +390,15 @@ def run_ours(a, dist: Dist):
     nb = cfg["NUM_BLOCKS"]
     buf_gb = 4 * nodes * (8 if fp64 else 4) / 1e9
     workload = ("%s: %dx%dx%d hex elements N=%d in %dx%dx%d blocks, %s, water, tone burst, adv+LDG diffusion+sponge"
-                % ("config2" if not a.elements else "config2 physics, resized", ne_g[0], ne_g[1], ne_g[2],
+                % ("config2" if not (a.elements or a.order) else "config2 physics, resized", ne_g[0], ne_g[1], ne_g[2],
                    cfg["ORDER"], nb[0], nb[1], nb[2], "FP64" if fp64 else "FP32"))
     ach = (st_b / st_n) / (st_ms / st_n / 1e3) / 1e9 if st_n else None
     traffic = profiled_traffic(kind)
     roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
             "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s",
-            "kernel": ("stage_kernel<double,%d,DIFF,2,EO> (fluxes read, even-odd line owners)" % (cfg["ORDER"] + 1)
+            "kernel": (("stage_kernel<double,5,DIFF,2,EO> (fluxes read, even-odd line owners)" if cfg["ORDER"] == 4
+                        else "stage_kernel<double,%d,DIFF,2> (fluxes read, per-node line sums)" % (cfg["ORDER"] + 1))
                        if fp64 else "incr_stage_kernel<float,%d,DIFF>" % (cfg["ORDER"] + 1)),
             "algorithmic_bytes_per_launch": st_b / st_n if st_n else None,
             "traffic_note": ("above the algorithmic bytes by the volume-flux buffers (4 values written and 4 read "
@@ -406,8 +412,9 @@ def run_ours(a, dist: Dist):
                                   "flops counted by the direct formula (K (K + 2) per line), which the even-odd "
                                   "line owners execute with about 22 % fewer FP64 instructions"},
             "share_of_step": st_ms / ms if ms else None,
-            "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<%d>" if fp64 else "ldg_gradient_kernel<float,%d>")
-                                        % (cfg["ORDER"] + 1),
+            "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<5>" if fp64 and cfg["ORDER"] == 4 else
+                                         ("ldg_gradient_kernel<double,%d>" if fp64 else "ldg_gradient_kernel<float,%d>")
+                                         % (cfg["ORDER"] + 1)),
                                 "launches": gr_n, "mean_launch_ms": gr_ms / gr_n if gr_n else None,
                                 "achieved_gbs": (gr_b / gr_n) / (gr_ms / gr_n / 1e3) / 1e9 if gr_n else None}}
     line = {
