@@ -52,6 +52,35 @@ __device__ __forceinline__ float batch_in(const BatchProblem& P, const float* ub
     return v;
 }
 
+// Face-table codes of the face nodes this thread evaluates in the pass whose
+// first element is c0 (0 where it has none).
+template <int K, int R>
+__device__ __forceinline__ void batch_codes(const BatchProblem& P, const BatchTile& T, int c0, int slot, int n,
+                                            int code[R])
+{
+    constexpr int NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K * K;
+    const int e = c0 + slot;
+    const bool live = slot < EPB && e < T.e0 + T.count;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int t = n + r * NPT;
+        code[r] = 0;
+        if (live && t < NF) {
+            const FaceNodeArith<K> F(t);
+            code[r] = __ldg(P.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        }
+    }
+}
+
+template <int K>
+__device__ __forceinline__ float batch_sigma(const BatchProblem& P, const BatchTile& T, int c0, int slot, int n)
+{
+    constexpr int NPT = npt_of(K), EPB = bepb_of(K), K3 = K * K * K;
+    const int e = c0 + slot;
+    return (slot < EPB && e < T.e0 + T.count && n < K3) ? __ldg(P.sigma + e) : 0.f;
+    (void)NPT;
+}
+
 template <int K>
 __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, const BatchTile& T, int stage,
                                 unsigned char* smraw)
@@ -62,23 +91,21 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
     const float* ub = P.u[P.cur];
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
+    // Face nodes assigned densely (see stage_kernel).  The face-table codes
+    // of each pass are loaded during the pass before, so a pass's neighbour
+    // loads wait on one memory latency instead of two chained ones.
+    int code_next[R];
+    batch_codes<K, R>(P, T, T.e0, slot, n, code_next);
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
         const int e = c0 + slot;
         const bool live = slot < EPB && e < T.e0 + T.count;
         const bool act = live && n < K3;
         GradSmem<float, K>& S = SM[slot < EPB ? slot : 0];
-        // Face nodes assigned densely (see stage_kernel); every global load
-        // is issued before the first use (the kernel waits on memory latency).
         int code[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int t = n + r * NPT;
-            code[r] = 0;
-            if (live && t < NF) {
-                const FaceNodeArith<K> F(t);
-                code[r] = __ldg(P.nbr + (size_t)e * 6 + 2 * F.a + F.side);
-            }
-        }
+        for (int r = 0; r < R; r++) code[r] = code_next[r];
+        batch_codes<K, R>(P, T, c0 + EPB, slot, n, code_next);
+        // every other global load is issued before the first use
         float rho = 0.f;
         if (act) rho = batch_in<K>(P, ub, inc, 0, (size_t)e * P.np + n);
         float ro[R];
@@ -159,27 +186,28 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
     const bool final_stage = stage == 2;
     float* dout = final_stage ? P.u[P.cur ^ 1] : P.d[stage];
     const float ca = P.ca[stage], cb = P.cb[stage], eps = final_stage ? P.eps : 0.f;
+    // The face-table codes and sigma of each pass are loaded during the pass
+    // before, so a pass's neighbour loads wait on one memory latency instead
+    // of two chained ones.
+    int code_next[R];
+    batch_codes<K, R>(P, T, T.e0, slot, n, code_next);
+    float sig_next = batch_sigma<K>(P, T, T.e0, slot, n);
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
         const int e = c0 + slot;
         const bool live = slot < EPB && e < T.e0 + T.count;
         const bool act = live && n < K3;
         PlainSmem<float, K>& S = SM[slot < EPB ? slot : 0];
         const size_t off = (size_t)e * P.np + n;
-        // Every global load before the first use (the kernel waits on memory
-        // latency): face-table codes and sigma, the own u, d, gradient and
-        // compensation, then the neighbour values of the densely assigned
-        // face nodes (see stage_kernel).
         int code[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int t = n + r * NPT;
-            code[r] = 0;
-            if (live && t < NF) {
-                const FaceNodeArith<K> F(t);
-                code[r] = __ldg(P.nbr + (size_t)e * 6 + 2 * F.a + F.side);
-            }
-        }
-        const float sig = act ? __ldg(P.sigma + e) : 0.f;
+        for (int r = 0; r < R; r++) code[r] = code_next[r];
+        const float sig = sig_next;
+        batch_codes<K, R>(P, T, c0 + EPB, slot, n, code_next);
+        sig_next = batch_sigma<K>(P, T, c0 + EPB, slot, n);
+        // Every other global load before the first use (the kernel waits on
+        // memory latency): the own u, d, gradient and compensation, then the
+        // neighbour values of the densely assigned face nodes (see
+        // stage_kernel).
         float ubv[4] = {0.f, 0.f, 0.f, 0.f}, dv[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
         float q[3] = {0.f, 0.f, 0.f};
         if (act) {
