@@ -63,6 +63,8 @@ def args_():
     ap.add_argument("--serve-baseline-rates", type=float, nargs="*", default=[15.0, 100.0])
     ap.add_argument("--serve-baseline-requests", type=int, default=24,
                     help="first requests of a trace served one at a time through the FP64 plain path")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving form (a rate sweep) and print its JSON object")
     return ap.parse_args()
 
 
@@ -654,6 +656,11 @@ def main():
     try:
         if a.impl == "reference":
             line = run_reference(a, dist)
+        elif a.serve_only:
+            line = None
+            if dist.rank == 0:
+                line = {"serving_form": serving_form(a, importlib.import_module("3ddg_gb300"),
+                                                     importlib.import_module("3ddg_gb300.workloads"))}
         else:
             line = run_ours(a, dist)
             if line is not None and dist.rank == 0 and dist.world == 1 and a.cpu_seconds > 0:
