@@ -600,7 +600,7 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 template <int K>
 __host__ __device__ constexpr bool eo_lines()
 {
-    return K == 5;  // at K = 4 they measured no faster than per-node sums
+    return K == 5;  // at K = 4 and K = 6 they measured no faster than per-node sums
 }
 
 template <int K>
@@ -1294,66 +1294,30 @@ __global__ void unpack_host_order_kernel(T* __restrict__ state, size_t fs, int n
     }
 }
 
-// Host-order device staging -> state, as a tiled transpose.  A CTA takes
-// up to CZ consecutive elements along z of one element row (block, local x,
-// local y): their nodes are K^2 host-order rows of CZ K contiguous values per
-// field, which the CTA reads coalesced into shared memory, and CZ NP
-// contiguous state slots, which it writes coalesced.  The fields are staged
-// one at a time; drho stays in shared memory for the velocities' mass fluxes.
-// Padding slots (n >= K^3) are not written.  For device memory only; pinned
-// host memory is read by unpack_host_order_kernel.
-template <int K>
-__host__ __device__ constexpr int unpack_cz()
+// Host-order device staging -> state, walked in element order: the state
+// writes are contiguous per element and the scattered side is the read
+// (K-value runs along z), which costs less than partial-sector writes.  For
+// device memory only; pinned host memory is read by unpack_host_order_kernel.
+template <typename T>
+__global__ void unpack_elem_order_kernel(T* __restrict__ state, size_t fs, int np, GridMap g, int n_elem,
+                                         const double* __restrict__ rho, const double* __restrict__ vel, size_t gsize,
+                                         FluxOut<T> fo)
 {
-    return K <= 5 ? 16 : (K <= 6 ? 8 : 4);
-}
-
-template <typename T, int K>
-__global__ void __launch_bounds__(256) unpack_tiled_kernel(T* __restrict__ state, size_t fs, GridMap g,
-                                                           const double* __restrict__ rho,
-                                                           const double* __restrict__ vel, size_t gsize,
-                                                           FluxOut<T> fo)
-{
-    constexpr int K2 = K * K, K3 = K2 * K, NP = (K3 + 7) / 8 * 8, CZ = unpack_cz<K>(), W = CZ * K;
-    __shared__ T sd[K2][W];
-    __shared__ T su[K2][W];
-    const int nzc = (g.ne[2] + CZ - 1) / CZ;
-    int idx = blockIdx.x;
-    const int zc = idx % nzc;
-    idx /= nzc;
-    const int lj = idx % g.ne[1];
-    idx /= g.ne[1];
-    const int li = idx % g.ne[0];
-    const int blk = idx / g.ne[0];
-    const int bx = blk / (g.nb[1] * g.nb[2]), by = (blk / g.nb[2]) % g.nb[1], bz = blk % g.nb[2];
-    const int cz = min(CZ, g.ne[2] - zc * CZ);
-    const size_t e0 = (size_t)blk * g.elem_per_block + ((size_t)li * g.ne[1] + lj) * g.ne[2] + (size_t)zc * CZ;
-    const size_t Y = (size_t)g.E[1] * K, Z = (size_t)g.E[2] * K;
-    const size_t x0 = (size_t)(bx * g.ne[0] + li) * K, y0 = (size_t)(by * g.ne[1] + lj) * K;
-    const size_t z0 = (size_t)(bz * g.ne[2] + zc * CZ) * K;
-    const int w = cz * K;
-    for (int f = 0; f < 4; f++) {
-        const double* src = f == 0 ? rho : vel + (size_t)(f - 1) * gsize;
-        T(*s)[W] = f == 0 ? sd : su;
-        if (f > 1) __syncthreads();  // the previous velocity is written out
-        for (int t = threadIdx.x; t < K2 * W; t += blockDim.x) {
-            const int r = t / W, z = t % W;
-            if (z < w) s[r][z] = (T)src[((x0 + r / K) * Y + y0 + r % K) * Z + z0 + z];
+    const int K3 = g.K * g.K * g.K;
+    const size_t total = (size_t)n_elem * np;
+    for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < total; s += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(s / np), n = (int)(s % np);
+        if (n >= K3) continue;
+        const size_t i = grid_index(g, e, n);
+        const T d = (T)rho[i];
+        T u[3];
+        state[s] = d;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            u[a] = (T)vel[a * gsize + i];
+            state[(size_t)(1 + a) * fs + s] = u[a];
         }
-        __syncthreads();
-        T* dst = state + (size_t)f * fs + e0 * NP;
-        for (int t = threadIdx.x; t < cz * NP; t += blockDim.x) {
-            const int ek = t / NP, n = t % NP;
-            if (n >= K3) continue;
-            const int r = n / K, c = n % K;
-            const T v = s[r][ek * K + c];
-            dst[t] = v;
-            if (fo.f) {
-                const size_t o = e0 * NP + t;
-                if (f == 0) fo.f[o] = momentum_flux(v, fo.k1, fo.k2);
-                else fo.f[(size_t)f * fs + o] = mass_flux(v, sd[r][ek * K + c], fo.r0, fo.linear);
-            }
-        }
+        if (fo.f) write_fluxes(fo, fs, s, d, u);
     }
 }
 

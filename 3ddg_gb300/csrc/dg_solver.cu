@@ -573,28 +573,18 @@ int Solver::unpack_in(const double* drho, const double* vel)
     return DG_OK;
 }
 
+// Host-order device staging -> state on stream st, walked in element order.
 template <typename T>
-cudaError_t Solver::launch_unpack_tiled(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
-                                        const FluxOut<T>& fo, cudaStream_t st)
+cudaError_t Solver::launch_unpack_staged(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
+                                         const FluxOut<T>& fo, cudaStream_t st)
 {
-    const size_t fs = mesh.fstride();
-    const int nb = mesh.nb[0] * mesh.nb[1] * mesh.nb[2];
-    auto grid = [&](int cz) { return (unsigned)(nb * mesh.ne[0] * mesh.ne[1] * ((mesh.ne[2] + cz - 1) / cz)); };
-    switch (mesh.K) {
-    case 2: unpack_tiled_kernel<T, 2><<<grid(unpack_cz<2>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 3: unpack_tiled_kernel<T, 3><<<grid(unpack_cz<3>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 4: unpack_tiled_kernel<T, 4><<<grid(unpack_cz<4>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 5: unpack_tiled_kernel<T, 5><<<grid(unpack_cz<5>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 6: unpack_tiled_kernel<T, 6><<<grid(unpack_cz<6>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 7: unpack_tiled_kernel<T, 7><<<grid(unpack_cz<7>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    case 8: unpack_tiled_kernel<T, 8><<<grid(unpack_cz<8>()), 256, 0, st>>>(state, fs, g, rho_d, vel_d, gsize(), fo); break;
-    default: return cudaErrorInvalidValue;
-    }
+    unpack_elem_order_kernel<T><<<152 * 16, 256, 0, st>>>(state, mesh.fstride(), mesh.NP, g, mesh.n_elem, rho_d,
+                                                          vel_d, gsize(), fo);
     return cudaGetLastError();
 }
 
-// Host-order arrays -> state on the compute stream: device staging by the
-// tiled transpose, pinned host memory (read over the CPU-GPU link) in host
+// Host-order arrays -> state on the compute stream: device staging walked in
+// element order, pinned host memory (read over the CPU-GPU link) in host
 // order.
 int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_device)
 {
@@ -605,8 +595,8 @@ int Solver::launch_unpack(const double* rho_d, const double* vel_d, bool on_devi
     const FluxOut<double> fo = flux_consts<double>(d_flux[flux_cur], p.rho0, p.c0, p.b_over_a);
     const FluxOut<float> none = flux_consts<float>(nullptr, p.rho0, p.c0, p.b_over_a);
     if (on_device) {
-        cudaError_t e = fp64() ? launch_unpack_tiled<double>((double*)state_ptr(), g, rho_d, vel_d, fo, stream)
-                               : launch_unpack_tiled<float>((float*)state_ptr(), g, rho_d, vel_d, none, stream);
+        cudaError_t e = fp64() ? launch_unpack_staged<double>((double*)state_ptr(), g, rho_d, vel_d, fo, stream)
+                               : launch_unpack_staged<float>((float*)state_ptr(), g, rho_d, vel_d, none, stream);
         if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("unpack: ") + cudaGetErrorString(e));
     } else {
         if (fp64())
@@ -683,10 +673,10 @@ int Solver::set_state_async(const double* drho, const double* vel)
     cudaError_t e;
     if (fp64()) {
         const FluxOut<double> fo = flux_consts<double>(spare_f, p.rho0, p.c0, p.b_over_a);
-        e = launch_unpack_tiled<double>((double*)spare_u, g, st, st + n, fo, xin);
+        e = launch_unpack_staged<double>((double*)spare_u, g, st, st + n, fo, xin);
     } else {
         const FluxOut<float> none = flux_consts<float>(nullptr, p.rho0, p.c0, p.b_over_a);
-        e = launch_unpack_tiled<float>((float*)spare_u, g, st, st + n, none, xin);
+        e = launch_unpack_staged<float>((float*)spare_u, g, st, st + n, none, xin);
     }
     if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("unpack: ") + cudaGetErrorString(e));
     launches++;

@@ -94,8 +94,8 @@ struct Solver {
     int unpack_in(const double* drho, const double* vel);
     int launch_unpack(const double* rho_d, const double* vel_d, bool on_device);
     template <typename T>
-    cudaError_t launch_unpack_tiled(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
-                                    const FluxOut<T>& fo, cudaStream_t st);
+    cudaError_t launch_unpack_staged(T* state, const GridMap& g, const double* rho_d, const double* vel_d,
+                                     const FluxOut<T>& fo, cudaStream_t st);
 
     // Asynchronous host transfers (dg_set_state_async / dg_get_state_async):
     // copy-engine streams and double-buffered device staging, so that one

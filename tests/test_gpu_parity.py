@@ -475,9 +475,9 @@ def test_tiny_meshes_match_oracle(ne, periodic, order, solver_for, oracle_for):
                                          (7, (2, 1, 5), (1, 1, 2))])
 def test_set_state_round_trip_every_order(order, ne, nb, precision, solver_for):
     """dg_set_state from pageable memory goes through device staging and the
-    tiled transpose into the element-major state (z runs of 4, 8 or 16
-    elements per CTA, ragged at the end of a block row); reading it back gives
-    the same values (FP64: bitwise; FP32: the values rounded to float)."""
+    element-order unpack into the element-major state (multi-block meshes,
+    z extents that are not multiples of a tile); reading it back gives the
+    same values (FP64: bitwise; FP32: the values rounded to float)."""
     cfg = small(order=order, ne=ne)
     cfg["NUM_BLOCKS"] = list(nb)
     cfg["PRECISION"] = precision
