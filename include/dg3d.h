@@ -122,9 +122,11 @@ int dg_set_state(dg_handle* h, const double* drho, const double* vel);
  * host buffers (no counterpart in the reference, whose state never leaves the
  * host).  The copies run on the copy engines through double-buffered device
  * staging on two streams of their own, ordered against dg_step through
- * events, so that the upload of the next input and the download of the last
- * result overlap the steps computing between them.  dg_get_state_async
- * captures the state at its place in the call sequence.  Host buffers must
+ * events; an upload is unpacked on a high-priority stream into a spare state
+ * buffer that is swapped in at its place in the call sequence, and a download
+ * is packed on another, so that the upload of the next input and the download
+ * of the last result overlap the steps computing between them.
+ * dg_get_state_async captures the state at its place in the call sequence.  Host buffers must
  * stay untouched (inputs) or unread (outputs) until dg_synchronize returns.
  * Pageable buffers are rejected with DG_ERR_INVALID. */
 int dg_set_state_async(dg_handle* h, const double* drho, const double* vel);
@@ -257,7 +259,11 @@ int dg_kernel_stats(dg_handle* h, int k, long long* launches, double* ms, double
  * Writes through them must be ordered against the library's stream
  * (dg_stream) and made before the next dg_step; to write again after later
  * steps, call dg_state_device again first (the FP64 path caches the volume
- * fluxes of the state between stages, and this call drops that cache). */
+ * fluxes of the state between stages, and this call drops that cache).
+ * dg_set_state_async swaps in another state buffer: pointers taken before it
+ * are stale after it.  The library's stream is made to wait for a pending
+ * dg_get_state_async pack of the state, so writes ordered on dg_stream come
+ * after it. */
 int dg_state_device(dg_handle* h, void* base[4], size_t* node_stride, int* n_elem);
 
 /* ------------------------------------------------------------------------
