@@ -135,7 +135,14 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
         {
             constexpr int WPA = (K2 + 31) / 32;
             int a, t, ls;
-            if constexpr (K >= 5) {
+            if constexpr (K >= 6) {
+                // 3 K^2 = 108 tasks packed densely into 4 warps (an axis per
+                // lane; the rows do not depend on the axis) instead of two
+                // warps per axis with 28 idle lanes each
+                a = n / K2;
+                t = n % K2;
+                ls = slot;
+            } else if constexpr (K == 5) {
                 const int w = n / 32;
                 a = w / WPA;
                 t = (w % WPA) * 32 + n % 32;
@@ -268,12 +275,20 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
         __syncthreads();
         {
             // Line owners (see incr_stage_kernel); the per-axis results, already
-            // times 1/w_a, reuse S.m (density) and S.q (momentum).  K >= 5: one
-            // warp (two for K = 6) per axis of each element slot, a lane per
-            // line; K <= 4: the CTA's threads over (slot, axis, line).
+            // times 1/w_a, reuse S.m (density) and S.q (momentum).  K = 5: one
+            // warp per axis of each element slot, a lane per line; K = 6: the
+            // element's 108 lines over its first 4 warps; K <= 4: the CTA's
+            // threads over (slot, axis, line).
             constexpr int WPA = (K2 + 31) / 32;
             int a, t, ls;
-            if constexpr (K >= 5) {
+            if constexpr (K >= 6) {
+                // 3 K^2 = 108 tasks packed densely into 4 warps (an axis per
+                // lane; the rows do not depend on the axis) instead of two
+                // warps per axis with 28 idle lanes each
+                a = n / K2;
+                t = n % K2;
+                ls = slot;
+            } else if constexpr (K == 5) {
                 const int w = n / 32;
                 a = w / WPA;
                 t = (w % WPA) * 32 + n % 32;
