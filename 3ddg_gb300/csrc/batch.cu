@@ -203,7 +203,13 @@ int Batch::init(int device_capacity)
     capacity = std::max(16, device_capacity);
     DGB_CUDA(cudaMallocFromPoolAsync((void**)&d_probs, capacity * sizeof(BatchProblem), pool, stream));
     DGB_CUDA(cudaStreamSynchronize(stream));
+    // Default tile sizes: the autotuner's choice on the 256-instance batch of
+    // uneven problems (32, 64, 16 and 8 elements per tile at K = 3, 4, 5, 6),
+    // which a batch that is not tuned itself (a server's) starts from.
     for (int k = 0; k <= BATCH_KMAX; k++) passes[k] = 4;
+    passes[4] = 16;
+    passes[5] = 8;
+    passes[6] = 8;
     return DG_OK;
 }
 
