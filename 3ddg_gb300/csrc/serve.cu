@@ -49,18 +49,21 @@ struct Server {
     struct TickRec {
         cudaEvent_t start = nullptr, end = nullptr, post = nullptr;
         int k = 0;
-        std::vector<long long> done;
+        std::vector<Req*> done;
     };
 
     Batch batch;
     size_t budget = 0, in_use = 0;
     bool keep_results = false;
-    std::map<long long, Req> reqs;   // inserted only by submit (under mu)
-    std::deque<long long> pending;   // submitted, not yet admitted (arrival order)
-    std::vector<long long> inflight; // batch index -> request id
+    // Requests by id, inserted by submit under mu (map nodes never move, so
+    // the loop keeps plain pointers to them).  The fields a reader of results
+    // or statistics sees (times, results, counters) are written under mu.
+    std::map<long long, Req> reqs;
+    std::deque<Req*> pending;        // loop thread: submitted, not yet admitted (arrival order)
+    std::vector<Req*> inflight;      // loop thread: batch index -> request
     std::deque<TickRec> outstanding; // ticks enqueued, not yet seen complete
     std::vector<cudaEvent_t> timing_events, plain_events;
-    long long next_id = 1;
+    long long next_id = 1;           // under mu
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     cudaEvent_t base_ev = nullptr;   // host time t_base on the device timeline
     double t_base = 0.0;
@@ -76,7 +79,8 @@ struct Server {
     // worker thread: builds arriving requests' meshes ahead of admission
     std::mutex mu;
     std::condition_variable cv_work, cv_ready;
-    std::deque<long long> to_prepare;  // arrival order
+    std::deque<Req*> to_prepare;  // arrival order
+    std::vector<Req*> incoming;   // submitted from any thread, not yet seen by the loop
     int prepared_ahead = 0;
     bool stop = false;
     std::thread worker;
@@ -111,7 +115,7 @@ struct Server {
                 std::unique_lock<std::mutex> lock(mu);
                 cv_work.wait(lock, [&] { return stop || (!to_prepare.empty() && prepared_ahead < kPrepareAhead); });
                 if (stop) return;
-                r = &reqs[to_prepare.front()];
+                r = to_prepare.front();
                 to_prepare.pop_front();
                 prepared_ahead++;
             }
@@ -169,13 +173,14 @@ struct Server {
         t.start = t.end = t.post = nullptr;
     }
 
+    // Any thread: the request goes to the worker's preparation queue and to
+    // the incoming queue, which the loop drains at its next iteration.
     int submit(const dg_params& p, double dt, int steps, double t_arrival, long long* id)
     {
         std::string err = Batch::validate(p);
         if (!err.empty()) return fail(DG_ERR_INVALID, err);
         if (!(dt > 0.0) || steps < 1) return fail(DG_ERR_INVALID, "dg_serve_submit: dt must be > 0 and steps >= 1");
         Req r;
-        r.id = next_id++;
         r.p = p;
         r.p.precision = DG_PRECISION_FP32;
         r.dt = dt;
@@ -187,20 +192,43 @@ struct Server {
                                           " bytes, more than the whole HBM budget " + std::to_string(budget));
         r.t_arrival = t_arrival < 0.0 ? now() : t_arrival;
         const double ta = r.t_arrival;
-        // keep pending and the preparation queue sorted by arrival time
-        auto it = pending.begin();
-        while (it != pending.end() && reqs[*it].t_arrival <= ta) ++it;
-        pending.insert(it, r.id);
         {
             std::lock_guard<std::mutex> lock(mu);
-            auto jt = to_prepare.begin();
-            while (jt != to_prepare.end() && reqs[*jt].t_arrival <= ta) ++jt;
-            to_prepare.insert(jt, r.id);
+            r.id = next_id++;
             if (id) *id = r.id;
-            reqs[r.id] = std::move(r);
+            const long long rid = r.id;
+            Req& slot = reqs[rid];
+            slot = std::move(r);
+            Req* rp = &slot;
+            // the preparation queue stays sorted by arrival time
+            auto jt = to_prepare.begin();
+            while (jt != to_prepare.end() && (*jt)->t_arrival <= ta) ++jt;
+            to_prepare.insert(jt, rp);
+            incoming.push_back(rp);
         }
         cv_work.notify_one();
         return DG_OK;
+    }
+
+    // Loop thread: move submitted requests into pending, sorted by arrival.
+    void drain_incoming()
+    {
+        std::vector<Req*> in;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            in.swap(incoming);
+        }
+        for (Req* r : in) {
+            auto it = pending.begin();
+            while (it != pending.end() && (*it)->t_arrival <= r->t_arrival) ++it;
+            pending.insert(it, r);
+        }
+    }
+
+    bool has_incoming()
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        return !incoming.empty();
     }
 
     // Admit arrived, prepared requests in arrival order while their memory
@@ -208,7 +236,7 @@ struct Server {
     int admit(double t)
     {
         while (!pending.empty()) {
-            Req& r = reqs[pending.front()];
+            Req& r = *pending.front();
             if (r.t_arrival > t) break;
             if (in_use + r.bytes > budget) break;  // FIFO: later requests wait behind it
             std::unique_ptr<Batch::Prepared> pr;
@@ -224,8 +252,11 @@ struct Server {
             int rc = batch.commit(*pr, &idx);
             if (rc) return rc;
             in_use += r.bytes;
-            r.t_admit = now();
-            inflight.push_back(r.id);
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                r.t_admit = now();
+            }
+            inflight.push_back(&r);
             pending.pop_front();
         }
         return DG_OK;
@@ -243,9 +274,9 @@ struct Server {
     int steps_this_tick(double t)
     {
         int k = kMaxStepsPerTick;
-        for (long long id : inflight) k = std::min(k, reqs.at(id).remaining);
+        for (const Req* r : inflight) k = std::min(k, r->remaining);
         if (!pending.empty()) {
-            Req& f = reqs.at(pending.front());
+            const Req& f = *pending.front();
             const double wait = f.t_arrival - t;
             if (wait <= 0.0) {
                 // arrived: waiting for memory (freed by the next retirement)
@@ -278,11 +309,12 @@ struct Server {
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms_run, t.start, t.end);
         if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventElapsedTime: ") + cudaGetErrorString(e));
         const double t_end = t_base + ms_end * 1e-3;
-        busy_s += ms_run * 1e-3;
         const double per = ms_run * 1e-3 / t.k;
         step_s = step_s > 0.0 ? 0.8 * step_s + 0.2 * per : per;
-        for (long long id : t.done) {
-            Req& r = reqs[id];
+        std::lock_guard<std::mutex> lock(mu);
+        busy_s += ms_run * 1e-3;
+        for (Req* rp : t.done) {
+            Req& r = *rp;
             r.t_done = t_end;
             if (r.result) {
                 const size_t g = (size_t)r.dims[0] * r.dims[1] * r.dims[2];
@@ -316,6 +348,7 @@ struct Server {
     // ahead of the device, or to drain when nothing is in flight.
     int tick(int* n_inflight)
     {
+        drain_incoming();
         int rc = collect(false);
         if (rc) return rc;
         rc = admit(now());
@@ -334,15 +367,20 @@ struct Server {
             if (rc) return rc;
             e = cudaEventRecord(t.end, st);
             if (e != cudaSuccess) return fail(DG_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+            double w = 0.0;
             for (size_t i = 0; i < inflight.size(); i++) {
                 const Batch::Entry& E = batch.probs[i];
-                work += 4.0 * E.n_elem * E.K * E.K * E.K * 3.0 * k;
-                reqs[inflight[i]].remaining -= k;
+                w += 4.0 * E.n_elem * E.K * E.K * E.K * 3.0 * k;
+                inflight[i]->remaining -= k;
             }
-            ticks += k;
-            inflight_sum += (double)inflight.size() * k;
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                work += w;
+                ticks += k;
+                inflight_sum += (double)inflight.size() * k;
+            }
             for (int i = (int)inflight.size() - 1; i >= 0; i--) {
-                Req& r = reqs[inflight[i]];
+                Req& r = *inflight[i];
                 if (r.remaining > 0) continue;
                 const Batch::Entry& E = batch.probs[i];
                 for (int a = 0; a < 3; a++) r.dims[a] = E.dims[a];
@@ -357,7 +395,7 @@ struct Server {
                 rc = batch.remove(i);
                 if (rc) return rc;
                 in_use -= r.bytes;
-                t.done.push_back(r.id);
+                t.done.push_back(&r);
                 inflight.erase(inflight.begin() + i);
             }
             e = cudaEventRecord(t.post, st);
@@ -373,10 +411,12 @@ struct Server {
     int run(double max_seconds)
     {
         const double t_end = now() + (max_seconds > 0 ? max_seconds : 1e300);
-        while (!pending.empty() || !inflight.empty() || !outstanding.empty()) {
+        drain_incoming();
+        while (!pending.empty() || !inflight.empty() || !outstanding.empty() || has_incoming()) {
             if (now() > t_end) return fail(DG_ERR_STATE, "dg_serve_run: time limit reached");
+            drain_incoming();
             if (inflight.empty() && !pending.empty()) {
-                Req& f = reqs[pending.front()];
+                Req& f = *pending.front();
                 const double wait = f.t_arrival - now();
                 if (wait > 0) {
                     std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
@@ -446,6 +486,7 @@ int dg_serve_result(dg_server* s, long long id, double* t_arrival, double* t_adm
                     double* vel)
 {
     if (!s) return dg::fail(DG_ERR_INVALID, "dg_serve_result: null handle");
+    std::lock_guard<std::mutex> lock(s->s.mu);
     auto it = s->s.reqs.find(id);
     if (it == s->s.reqs.end()) return dg::fail(DG_ERR_INVALID, "dg_serve_result: unknown request");
     const dg::Server::Req& r = it->second;
@@ -465,6 +506,7 @@ int dg_serve_stats(dg_server* s, int* completed, double* p50, double* p99, doubl
                    double* mean_inflight)
 {
     if (!s) return dg::fail(DG_ERR_INVALID, "dg_serve_stats: null handle");
+    std::lock_guard<std::mutex> lock(s->s.mu);
     std::vector<double> lat;
     double first = 1e300, last = 0.0;
     for (const auto& kv : s->s.reqs) {
@@ -492,6 +534,7 @@ int dg_serve_stats(dg_server* s, int* completed, double* p50, double* p99, doubl
 int dg_serve_utilization(dg_server* s, double* gpu_busy_s, double* span_s, double* dof_stage_updates)
 {
     if (!s) return dg::fail(DG_ERR_INVALID, "dg_serve_utilization: null handle");
+    std::lock_guard<std::mutex> lock(s->s.mu);
     double first = 1e300, last = 0.0;
     for (const auto& kv : s->s.reqs) {
         const dg::Server::Req& r = kv.second;

@@ -322,7 +322,10 @@ int dg_serve_submit(dg_server* s, const dg_params* p, double dt, int steps, doub
  * to the server's device memory pool).  Admission and retirement are
  * stream-ordered device work, so the host never synchronises the device for
  * them; it waits only to stay at most two ticks ahead of the device, and
- * drains when nothing is in flight.  Call submit and tick from one thread. */
+ * drains when nothing is in flight.  dg_serve_submit, dg_serve_result,
+ * dg_serve_stats and dg_serve_utilization may be called from any thread
+ * (submissions go through an internal queue that the loop drains at each
+ * iteration); dg_serve_tick and dg_serve_run from one thread at a time. */
 int dg_serve_tick(dg_server* s, int* n_inflight);
 /* Run the loop in real time until every submitted request has finished. */
 int dg_serve_run(dg_server* s, double max_seconds);

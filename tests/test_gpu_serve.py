@@ -100,3 +100,36 @@ def test_steady_stream_accounting():
     assert abs(u["dof_stage_updates"] - want) <= 1e-9 * want
     assert 0.0 < u["gpu_busy_s"] <= u["span_s"] * 1.001
     assert st["p99_s"] >= st["p50_s"] > 0.0
+
+
+def test_submissions_from_another_thread():
+    """dg_serve_submit from a second thread while the loop thread ticks: every
+    request is served, and each result is the same as alone (the submit path
+    goes through the server's internal queue)."""
+    import threading
+    import time
+    m = dg()
+    cfgs = requests(n=12, seed=31)
+    ids, done = [], threading.Event()
+    with m.Server(hbm_budget_bytes=4 << 30, keep_results=True) as srv:
+        def producer():
+            for c in cfgs:
+                ids.append(srv.submit(c))
+                time.sleep(0.002)
+            done.set()
+
+        th = threading.Thread(target=producer)
+        th.start()
+        deadline = time.time() + 120
+        while time.time() < deadline:
+            srv.tick()
+            if done.is_set() and len(ids) == len(cfgs) and all(srv.result(i)["done"] >= 0 for i in ids):
+                break
+        th.join()
+        res = [srv.result(i, state=True) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(cfgs)
+    for c, r in zip(cfgs, res):
+        assert r["done"] >= r["admit"] >= r["arrival"]
+        ra, va = alone(c)
+        assert np.array_equal(r["rho"], ra) and np.array_equal(r["vel"], va)
