@@ -437,6 +437,18 @@ void Batch::build_tiles()
         if (probs[a].K != probs[b].K) return probs[a].K > probs[b].K;
         return probs[a].op_key < probs[b].op_key;
     });
+    // Elements of each group (order and operator), so that a small group (few
+    // problems in flight) gets tiles small enough for about two waves of its
+    // persistent grid instead of leaving SMs idle; a large group keeps the
+    // tuned tile size.
+    std::vector<long long> group_elems;
+    for (size_t n = 0; n < order.size(); n++) {
+        const Entry& E = probs[order[n]];
+        if (n == 0 || probs[order[n - 1]].K != E.K || probs[order[n - 1]].op_key != E.op_key)
+            group_elems.push_back(0);
+        group_elems.back() += E.n_elem;
+    }
+    int chunk = 0;
     for (size_t n = 0; n < order.size(); n++) {
         const int i = order[n];
         const Entry& E = probs[i];
@@ -447,8 +459,10 @@ void Batch::build_tiles()
             g.begin = g.end = (int)tiles.size();
             std::memcpy(g.ops.rows, E.desc.rows, sizeof g.ops.rows);
             groups.push_back(g);
+            const long long waves2 = 2LL * num_sms * std::max(1, std::min(ctas_per_sm, occ_k[K][1]));
+            const long long fit = (group_elems[groups.size() - 1] + bepb_of(K) * waves2 - 1) / (bepb_of(K) * waves2);
+            chunk = bepb_of(K) * (int)std::max(1LL, std::min<long long>(std::max(1, passes[K]), fit));
         }
-        const int chunk = bepb_of(K) * std::max(1, passes[K]);
         for (int e0 = 0; e0 < E.n_elem; e0 += chunk) {
             BatchTile t;
             t.prob = E.slot;
