@@ -625,12 +625,10 @@ int Solver::ensure_async()
     // Each resource is created once; a call after a failed one resumes here.
     if (!copy_in) DG_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
     if (!copy_out) DG_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
-    if (!xin || !xout) {
-        int lo = 0, hi = 0;
-        DG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        if (!xin) DG_CUDA(cudaStreamCreateWithPriority(&xin, cudaStreamNonBlocking, hi));
-        if (!xout) DG_CUDA(cudaStreamCreateWithPriority(&xout, cudaStreamNonBlocking, hi));
-    }
+    // the transposes share the SMs with the steps at the compute stream's
+    // priority (a higher one measured slightly slower end to end)
+    if (!xin) DG_CUDA(cudaStreamCreateWithFlags(&xin, cudaStreamNonBlocking));
+    if (!xout) DG_CUDA(cudaStreamCreateWithFlags(&xout, cudaStreamNonBlocking));
     const size_t es = fp64() ? sizeof(double) : sizeof(float);
     if (!spare_u) DG_CUDA(cudaMalloc(&spare_u, 4 * mesh.fstride() * es));
     if (fp64() && d_flux[0] && !spare_f) DG_CUDA(cudaMalloc(&spare_f, 4 * mesh.fstride() * sizeof(double)));

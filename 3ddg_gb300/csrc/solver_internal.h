@@ -101,7 +101,7 @@ struct Solver {
     // copy-engine streams and double-buffered device staging, so that one
     // step's upload and the previous step's download run under compute.  The
     // transposes between staging and the element-major state run on two
-    // high-priority streams of their own: an upload is unpacked (xin) into a
+    // streams of their own (default priority): an upload is unpacked (xin) into a
     // spare state buffer (and, FP64 with advection, a spare flux buffer) that
     // the compute stream swaps in at the upload's place in the call sequence,
     // so the unpack runs under the step before; a download's pack (xout)

@@ -122,7 +122,7 @@ int dg_set_state(dg_handle* h, const double* drho, const double* vel);
  * host buffers (no counterpart in the reference, whose state never leaves the
  * host).  The copies run on the copy engines through double-buffered device
  * staging on two streams of their own, ordered against dg_step through
- * events; an upload is unpacked on a high-priority stream into a spare state
+ * events; an upload is unpacked on a stream of its own into a spare state
  * buffer that is swapped in at its place in the call sequence, and a download
  * is packed on another, so that the upload of the next input and the download
  * of the last result overlap the steps computing between them.
