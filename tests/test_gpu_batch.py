@@ -113,3 +113,34 @@ def test_autotune_keeps_results():
         b2.step(10)
         ref = b2.state(1)
     assert np.array_equal(tuned[0], ref[0])
+
+
+def test_batch_tiny_and_ragged_problems():
+    """Problems of 1 to 6 elements at every order the batch takes, all in one
+    batch: tiles shorter than a pass (EPB up to 8 elements), every face on the
+    boundary, the source face on each.  Each matches the single-problem FP32
+    path within the FP32 tolerance of the other batch tests."""
+    m = dg()
+    W = workloads()
+    base = W.config4(seed=13, n=1, steps=20)[0]
+    cfgs = []
+    for order in (1, 2, 3, 4, 5):
+        for ne in ((1, 1, 1), (1, 2, 3), (3, 1, 2)):
+            c = dict(base)
+            c["ORDER"] = order
+            c["NUM_ELEMENTS"] = list(ne)
+            c["BC_SPONGE_WIDTH"] = [1, 1, 1, 1, 0, 1]
+            c["STARTING_CORNER"] = [-0.5 * ne[0] * 0.25, -0.5 * ne[1] * 0.25, 0.0]
+            c["DT"] = W.cfl_dt(c)
+            c["STEPS"] = 20
+            cfgs.append(c)
+    with m.Batch(cfgs) as b:
+        b.step(20)
+        got = [b.state(i) for i in range(len(cfgs))]
+    for c, (r, v) in zip(cfgs, got):
+        with m.Solver(c) as s:
+            s.step(c["DT"], 20)
+            r1, v1 = s.state()
+        assert np.max(np.abs(r1)) > 0
+        assert max_rel(pressure(c, r), pressure(c, r1)) <= 2e-5, (c["ORDER"], c["NUM_ELEMENTS"])
+        assert max_rel(v, v1) <= 2e-5, (c["ORDER"], c["NUM_ELEMENTS"])

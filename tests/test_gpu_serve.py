@@ -133,3 +133,29 @@ def test_submissions_from_another_thread():
         assert r["done"] >= r["admit"] >= r["arrival"]
         ra, va = alone(c)
         assert np.array_equal(r["rho"], ra) and np.array_equal(r["vel"], va)
+
+
+def test_one_step_requests_and_budget_of_exactly_one():
+    """Requests of a single RK step, under a budget of exactly one request's
+    bytes: they run one at a time, each finishes, and each result equals the
+    batch run alone."""
+    m = dg()
+    cfgs = requests(n=4, seed=17)
+    for c in cfgs:
+        c["NUM_ELEMENTS"] = [3, 2, 4]
+        c["ORDER"] = 2
+        c["STEPS"] = 1
+    per = 24 * 32 * 23 * 4 + 24 * 28  # 24 elements of 27 nodes padded to 32 slots
+    with m.Server(hbm_budget_bytes=per, keep_results=True) as srv:
+        ids = [srv.submit(c, arrival_time=0.0) for c in cfgs]
+        for _ in range(100000):
+            srv.tick()  # a one-step request is admitted and retired within one tick
+            if all(srv.result(i)["done"] >= 0 for i in ids):
+                break
+        res = [srv.result(i, state=True) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(cfgs)
+    assert st["mean_inflight"] == 1.0  # every step ran with exactly one solve in flight
+    for c, r in zip(cfgs, res):
+        ra, va = alone(c)
+        assert np.array_equal(r["rho"], ra) and np.array_equal(r["vel"], va)
