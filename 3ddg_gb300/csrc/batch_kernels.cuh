@@ -81,102 +81,110 @@ __device__ __forceinline__ float batch_sigma(const BatchProblem& P, const BatchT
     (void)NPT;
 }
 
+// Line task of this thread in a pass of the gradient phase: element slot ls,
+// axis a, line t (false: no task).  K = 5: one warp per axis of each element
+// slot; K = 6: the element's 108 lines over its first 4 warps; K <= 4: the
+// CTA's threads over (slot, axis, line).
+template <int K>
+__device__ __forceinline__ bool batch_line_task(int slot, int n, int& ls, int& a, int& t)
+{
+    constexpr int K2 = K * K, WPA = (K2 + 31) / 32, EPB = bepb_of(K);
+    if constexpr (K >= 6) {
+        a = n / K2;
+        t = n % K2;
+        ls = slot;
+    } else if constexpr (K == 5) {
+        const int w = n / 32;
+        a = w / WPA;
+        t = (w % WPA) * 32 + n % 32;
+        ls = slot;
+    } else {
+        ls = threadIdx.x / (3 * K2);
+        a = (threadIdx.x / K2) % 3;
+        t = threadIdx.x % K2;
+    }
+    return ls < EPB && a < 3 && t < K2;
+}
+
+// Face-table codes of the two ends of the owner's line (element c0 + ls).
+template <int K>
+__device__ __forceinline__ void batch_end_codes(const BatchProblem& P, const BatchTile& T, int c0, bool task, int ls,
+                                                int a, int code[2])
+{
+    const int e = c0 + ls;
+    const bool live = task && e < T.e0 + T.count;
+    code[0] = live ? __ldg(P.nbr + (size_t)e * 6 + 2 * a) : 0;
+    code[1] = live ? __ldg(P.nbr + (size_t)e * 6 + 2 * a + 1) : 0;
+}
+
+// The gradient phase of one tile.  Each line owner loads the neighbour
+// values at its line's two ends and forms the two central face fluxes itself
+// (the values the face-node form staged in shared memory), so a pass has two
+// barriers; the owners' face-table codes of each pass are loaded during the
+// pass before.
 template <int K>
 __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, const BatchTile& T, int stage,
                                 unsigned char* smraw)
 {
-    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K), NF = 6 * K2;
-    constexpr int R = (NF + NPT - 1) / NPT;
+    constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
     GradSmem<float, K>* SM = reinterpret_cast<GradSmem<float, K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
     const float* ub = P.u[P.cur];
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
-    // Face nodes assigned densely (see stage_kernel).  The face-table codes
-    // of each pass are loaded during the pass before, so a pass's neighbour
-    // loads wait on one memory latency instead of two chained ones.
-    int code_next[R];
-    batch_codes<K, R>(P, T, T.e0, slot, n, code_next);
+    int ls = 0, a = 0, t = 0;
+    const bool task = batch_line_task<K>(slot, n, ls, a, t);
+    const int st = axis_stride<K>(a < 3 ? a : 0);
+    const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
+    int code_next[2];
+    batch_end_codes<K>(P, T, T.e0, task, ls, a, code_next);
     for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
         const int e = c0 + slot;
-        const bool live = slot < EPB && e < T.e0 + T.count;
-        const bool act = live && n < K3;
-        GradSmem<float, K>& S = SM[slot < EPB ? slot : 0];
-        int code[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) code[r] = code_next[r];
-        batch_codes<K, R>(P, T, c0 + EPB, slot, n, code_next);
+        const bool act = slot < EPB && e < T.e0 + T.count && n < K3;
+        const bool owner = task && c0 + ls < T.e0 + T.count;
+        const int code[2] = {code_next[0], code_next[1]};
+        batch_end_codes<K>(P, T, c0 + EPB, task, ls, a, code_next);
         // every other global load is issued before the first use
         float rho = 0.f;
         if (act) rho = batch_in<K>(P, ub, inc, 0, (size_t)e * P.np + n);
-        float ro[R];
+        float ro[2] = {0.f, 0.f};
+        if (owner) {
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            ro[r] = 0.f;
-            const int t = n + r * NPT;
-            if (!live || t >= NF) continue;
-            const FaceNodeArith<K> F(t);
-            if (code[r] >= 0) {
-                ro[r] = batch_in<K>(P, ub, inc, 0, (size_t)code[r] * P.np + F.nn);
-            } else {
-                float uo;
-                batch_exterior(P, -1 - code[r], stage, ro[r], uo);
-            }
-        }
-        if (slot < EPB) S.r[n] = rho;
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int t = n + r * NPT;
-            if (!live || t >= NF) continue;
-            const FaceNodeArith<K> F(t);
-            S.fl[F.a][F.side][F.fi] = (F.side ? -0.5f : 0.5f) * (ro[r] + S.r[F.nf]);
-        }
-        __syncthreads();
-        {
-            constexpr int WPA = (K2 + 31) / 32;
-            int a, t, ls;
-            if constexpr (K >= 6) {
-                // 3 K^2 = 108 tasks packed densely into 4 warps (an axis per
-                // lane; the rows do not depend on the axis) instead of two
-                // warps per axis with 28 idle lanes each
-                a = n / K2;
-                t = n % K2;
-                ls = slot;
-            } else if constexpr (K == 5) {
-                const int w = n / 32;
-                a = w / WPA;
-                t = (w % WPA) * 32 + n % 32;
-                ls = slot;
-            } else {
-                ls = threadIdx.x / (3 * K2);
-                a = (threadIdx.x / K2) % 3;
-                t = threadIdx.x % K2;
-            }
-            GradSmem<float, K>& S = SM[ls < EPB ? ls : 0];
-            if (ls < EPB && c0 + ls < T.e0 + T.count && a < 3 && t < K2) {
-                const int st = axis_stride<K>(a);
-                const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
-                float v[K];
-#pragma unroll
-                for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
-                const float f0 = S.fl[a][0][t], fN = S.fl[a][1][t];
-                const float gs = P.gscale[a];
-#pragma unroll
-                for (int i = 0; i < K; i++) {
-                    const float* row = ops.rows[i];  // constant-bank operands
-                    float s2 = row[K] * f0;
-                    s2 += row[K + 1] * fN;
-#pragma unroll
-                    for (int j = 0; j < K; j++) s2 += row[j] * v[j];
-                    S.out[a][b0 + i * st] = gs * s2;
+            for (int side = 0; side < 2; side++) {
+                if (code[side] >= 0) {
+                    const size_t o2 = (size_t)code[side] * P.np + b0 + (side ? 0 : (K - 1) * st);
+                    ro[side] = batch_in<K>(P, ub, inc, 0, o2);
+                } else {
+                    float uo;
+                    batch_exterior(P, -1 - code[side], stage, ro[side], uo);
                 }
             }
-            __syncthreads();
         }
+        if (slot < EPB) SM[slot].r[n] = rho;
+        __syncthreads();
+        if (owner) {
+            GradSmem<float, K>& S = SM[ls];
+            float v[K];
+#pragma unroll
+            for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+            const float f0 = 0.5f * (ro[0] + v[0]), fN = -0.5f * (ro[1] + v[K - 1]);
+            const float gs = P.gscale[a];
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                const float* row = ops.rows[i];  // constant-bank operands
+                float s2 = row[K] * f0;
+                s2 += row[K + 1] * fN;
+#pragma unroll
+                for (int j = 0; j < K; j++) s2 += row[j] * v[j];
+                S.out[a][b0 + i * st] = gs * s2;
+            }
+        }
+        __syncthreads();
+        // no barrier before the next pass: it writes S.r (read above before
+        // the second barrier) and S.out only after its first barrier, which
+        // every thread reaches after these reads
         if (act)
 #pragma unroll
-            for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = S.out[a2][n];
-        __syncthreads();
+            for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = SM[slot].out[a2][n];
     }
 }
 
