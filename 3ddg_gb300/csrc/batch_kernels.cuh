@@ -357,7 +357,9 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
                 }
             }
         }
-        __syncthreads();
+        // no barrier before the next pass: a thread reads only its own node's
+        // S.m / S.q entries here, and the next pass rewrites them (by the same
+        // thread) before its first barrier and the other entries only after it
     }
 }
 
