@@ -324,6 +324,8 @@ int Batch::commit(Prepared& pr, int* index)
 {
     if (!pr.host) return fail(DG_ERR_STATE, "batch: problem not prepared");
     Entry E = pr.E;
+    // the problem's memory first, so that a failed admission takes no slot
+    DGB_CUDA(cudaMallocFromPoolAsync(&E.chunk, E.chunk_bytes, pool, stream));
     int slot;
     if (!free_slots.empty()) {
         slot = free_slots.back();
@@ -333,8 +335,14 @@ int Batch::commit(Prepared& pr, int* index)
             // grow the descriptor array in stream order
             const int ncap = capacity * 2;
             BatchProblem* nd = nullptr;
-            DGB_CUDA(cudaMallocFromPoolAsync((void**)&nd, ncap * sizeof(BatchProblem), pool, stream));
-            DGB_CUDA(cudaMemcpyAsync(nd, d_probs, slot_hi * sizeof(BatchProblem), cudaMemcpyDeviceToDevice, stream));
+            cudaError_t e = cudaMallocFromPoolAsync((void**)&nd, ncap * sizeof(BatchProblem), pool, stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(nd, d_probs, slot_hi * sizeof(BatchProblem), cudaMemcpyDeviceToDevice, stream);
+            if (e != cudaSuccess) {
+                if (nd) cudaFreeAsync(nd, stream);
+                cudaFreeAsync(E.chunk, stream);
+                return fail(DG_ERR_CUDA, std::string("batch: descriptor array: ") + cudaGetErrorString(e));
+            }
             DGB_CUDA(cudaFreeAsync(d_probs, stream));
             d_probs = nd;
             capacity = ncap;
@@ -342,7 +350,6 @@ int Batch::commit(Prepared& pr, int* index)
         }
         slot = slot_hi++;
     }
-    DGB_CUDA(cudaMallocFromPoolAsync(&E.chunk, E.chunk_bytes, pool, stream));
     unsigned char* c = (unsigned char*)E.chunk;
     E.data = c;
     E.nbr = (int*)(c + pr.data_bytes);

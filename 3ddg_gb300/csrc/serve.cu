@@ -42,6 +42,7 @@ struct Server {
         bool prep_done = false;
         int prep_rc = 0;
         std::string prep_err;
+        bool failed = false;  // preparation failed; never admitted
         PinnedPool::Block* result = nullptr;  // result copy in flight
     };
     // One tick's device work: its RK steps between two timing events, then
@@ -245,12 +246,25 @@ struct Server {
                 if (!r.prep_done) break;
                 pr = std::move(r.prep);
                 prepared_ahead--;
-                if (r.prep_rc) return fail(r.prep_rc, r.prep_err);
+                if (r.prep_rc) {
+                    // its preparation failed: set it aside (dg_serve_result
+                    // reports the error) and go on with the others
+                    r.failed = true;
+                    pending.pop_front();
+                    continue;
+                }
             }
             cv_work.notify_one();
             int idx = -1;
-            int rc = batch.commit(*pr, &idx);
-            if (rc) return rc;
+            int rc = pr ? batch.commit(*pr, &idx) : fail(DG_ERR_STATE, "serve: request has no preparation");
+            if (rc) {
+                // keep the prepared request for a later attempt (the error
+                // stands for this call)
+                std::lock_guard<std::mutex> lock(mu);
+                r.prep = std::move(pr);
+                prepared_ahead++;
+                return rc;
+            }
             in_use += r.bytes;
             {
                 std::lock_guard<std::mutex> lock(mu);
@@ -490,6 +504,7 @@ int dg_serve_result(dg_server* s, long long id, double* t_arrival, double* t_adm
     auto it = s->s.reqs.find(id);
     if (it == s->s.reqs.end()) return dg::fail(DG_ERR_INVALID, "dg_serve_result: unknown request");
     const dg::Server::Req& r = it->second;
+    if (r.failed) return dg::fail(r.prep_rc, "dg_serve_result: request failed: " + r.prep_err);
     if (t_arrival) *t_arrival = r.t_arrival;
     if (t_admit) *t_admit = r.t_admit;
     if (t_done) *t_done = r.t_done;

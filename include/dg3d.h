@@ -330,7 +330,9 @@ int dg_serve_tick(dg_server* s, int* n_inflight);
 /* Run the loop in real time until every submitted request has finished. */
 int dg_serve_run(dg_server* s, double max_seconds);
 /* Arrival, admission and completion times of a request; its final state when
- * the server keeps results (drho/vel may be NULL). */
+ * the server keeps results (drho/vel may be NULL).  A request whose host
+ * preparation failed is set aside (the loop goes on with the others) and
+ * returns that error here. */
 int dg_serve_result(dg_server* s, long long id, double* t_arrival, double* t_admit, double* t_done,
                     double* drho, double* vel);
 /* Completed requests, p50/p99 latency (s), completed solves per second over
