@@ -85,6 +85,7 @@ def lib():
             "dg_set_state": (i, [vp, vp, vp]),
             "dg_set_state_async": (i, [vp, vp, vp]),
             "dg_get_state_async": (i, [vp, vp, vp]),
+            "dg_step_get_state_async": (i, [vp, d, vp, vp]),
             "dg_eval_rhs": (i, [vp, vp, vp]),
             "dg_eval_rhs_noalloc": (i, [C.POINTER(DgParams), vp, vp, vp, vp, vp, vp, i, vp]),
             "dg_get_grid": (i, [vp, vp, vp]),
@@ -256,6 +257,15 @@ class Solver:
             if not (a.flags.c_contiguous and a.dtype == np.float64):
                 raise DGError("set_state_async needs C-contiguous float64 arrays")
         _check(lib().dg_set_state_async(self.h, _ptr(rho), _ptr(vel)), "dg_set_state_async")
+
+    def step_state_async(self, dt: float, rho, vel):
+        """One RK step, then a download of its result into pinned, C-contiguous
+        float64 arrays (dg_step_get_state_async); they hold the state after
+        ``synchronize``."""
+        for a in (rho, vel):
+            if not (a.flags.c_contiguous and a.dtype == np.float64):
+                raise DGError("step_state_async needs C-contiguous float64 arrays")
+        _check(lib().dg_step_get_state_async(self.h, float(dt), _ptr(rho), _ptr(vel)), "dg_step_get_state_async")
 
     def state_async(self, rho, vel):
         """Queue a download into pinned, C-contiguous float64 arrays (either may

@@ -109,6 +109,24 @@ struct MeshDev {
     T src_p;               // source pressure at this stage's time
 };
 
+// Element-major state  <->  node-duplicated [X][Y][Z] grid layout (the
+// reference's HDF5 dataset order, cppsrc/HDF5Functions.cpp:173-208).
+struct GridMap {
+    int K, nb[3], ne[3], E[3], elem_per_block;
+};
+
+__device__ __forceinline__ size_t grid_index(const GridMap& g, int e, int n)
+{
+    const int blk = e / g.elem_per_block, le = e % g.elem_per_block;
+    const int b0 = blk / (g.nb[1] * g.nb[2]), b1 = (blk / g.nb[2]) % g.nb[1], b2 = blk % g.nb[2];
+    const int l0 = le / (g.ne[1] * g.ne[2]), l1 = (le / g.ne[2]) % g.ne[1], l2 = le % g.ne[2];
+    const int K = g.K;
+    const size_t ii = (size_t)(b0 * g.ne[0] + l0) * K + n / (K * K);
+    const size_t jj = (size_t)(b1 * g.ne[1] + l1) * K + (n / K) % K;
+    const size_t kk = (size_t)(b2 * g.ne[2] + l2) * K + n % K;
+    return (ii * ((size_t)g.E[1] * K) + jj) * ((size_t)g.E[2] * K) + kk;
+}
+
 // Stage input/output.  R' = ca R_ops is what the folded operator produces
 // (R_ops: advection + diffusion, without the sponge).
 //   PLAIN (FP64 method), stage input s = ``src``:
@@ -135,6 +153,11 @@ struct StageIO {
     int np;                // nodes per element in memory
     T ca, cb, cc, eps;
     int final_stage;
+    // PLAIN, PACK: the output also written in host order ([X][Y][Z] per
+    // field, fields gsize apart) for a download
+    double* pack;
+    GridMap pack_map;
+    size_t pack_gsize;
 };
 
 template <typename T>
@@ -729,7 +752,11 @@ __device__ __forceinline__ void stage_eo_line(const LineEOAxis<K>& X, PlainSmem<
 // rows in registers); true (D centro-antisymmetric, see LineEO), line owners
 // apply the even-odd operator after the face phase, one more barrier, and
 // each node adds its three axis results.
-template <typename T, int K, bool DIFF, int FLUX, bool EO>
+//
+// PACK: the stage's output is also written in host order to io.pack (the
+// last stage of a step whose result is downloaded: the pack rides on the
+// FP64-bound stage instead of a kernel of its own).
+template <typename T, int K, bool DIFF, int FLUX, bool EO, bool PACK = false>
 __global__ void __launch_bounds__(npt_of(K) * plain_epb<K, EO>(), (plain_min_blocks<T, K, EO>()))
 stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, const LineEO<K> L, int do_adv,
              int do_sponge)
@@ -904,6 +931,11 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
 #pragma unroll
         for (int a = 0; a < 3; a++)
             io.flux_out[(size_t)(1 + a) * io.fs + off] = mass_flux(vo[1 + a], vo[0], C.r0, C.linear_mass);
+    }
+    if constexpr (PACK) {
+        const size_t gi = grid_index(io.pack_map, e, n);
+#pragma unroll
+        for (int f = 0; f < 4; f++) io.pack[(size_t)f * io.pack_gsize + gi] = (double)vo[f];
     }
 }
 
@@ -1208,24 +1240,6 @@ inline bool make_line_eo(const OpConst<double, K>& C, LineEO<K>& L)
         L.ax[a].Lm = (K & 1) ? R[H][K] : 0.0;
     }
     return true;
-}
-
-// Element-major state  <->  node-duplicated [X][Y][Z] grid layout (the
-// reference's HDF5 dataset order, cppsrc/HDF5Functions.cpp:173-208).
-struct GridMap {
-    int K, nb[3], ne[3], E[3], elem_per_block;
-};
-
-__device__ __forceinline__ size_t grid_index(const GridMap& g, int e, int n)
-{
-    const int blk = e / g.elem_per_block, le = e % g.elem_per_block;
-    const int b0 = blk / (g.nb[1] * g.nb[2]), b1 = (blk / g.nb[2]) % g.nb[1], b2 = blk % g.nb[2];
-    const int l0 = le / (g.ne[1] * g.ne[2]), l1 = (le / g.ne[2]) % g.ne[1], l2 = le % g.ne[2];
-    const int K = g.K;
-    const size_t ii = (size_t)(b0 * g.ne[0] + l0) * K + n / (K * K);
-    const size_t jj = (size_t)(b1 * g.ne[1] + l1) * K + (n / K) % K;
-    const size_t kk = (size_t)(b2 * g.ne[2] + l2) * K + n % K;
-    return (ii * ((size_t)g.E[1] * K) + jj) * ((size_t)g.E[2] * K) + kk;
 }
 
 // State <-> host-order arrays rho [X][Y][Z], vel [3][X][Y][Z], walked in host

@@ -158,22 +158,30 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
 // FP64 stage kernel in the flux mode that io asks for (flux_out: write the
 // output's volume fluxes; flux_in: read the input's), with even-odd line
 // owners where the order has them and the operator allows them.
-template <typename T, int K, bool DIFF, bool EO, int FLUX>
+template <typename T, int K, bool DIFF, bool EO, int FLUX, bool PACK = false>
 void launch_plain_eo(const Solver& s, const StageIO<T>& io, const MeshDev<T>& md, const OpConst<T, K>* Cp,
                      const LineEO<K>& L)
 {
     const dim3 block(npt_of(K), plain_epb<K, EO>());
     const dim3 grid((md.n_elem + plain_epb<K, EO>() - 1) / plain_epb<K, EO>());
-    stage_kernel<T, K, DIFF, FLUX, EO><<<grid, block, 0, s.stream>>>(io, md, Cp, L, s.p.eval_advect, s.p.eval_sponge);
+    stage_kernel<T, K, DIFF, FLUX, EO, PACK><<<grid, block, 0, s.stream>>>(io, md, Cp, L, s.p.eval_advect,
+                                                                          s.p.eval_sponge);
 }
 
+// The host-order pack rides only on the flux-reading mode (the steady state
+// of stepping with advection); io.pack is set only when that mode runs.
 template <typename T, int K, bool DIFF, bool EO>
 void launch_plain_mode(const Solver& s, const StageIO<T>& io, const MeshDev<T>& md, const OpConst<T, K>* Cp,
                        const LineEO<K>& L)
 {
-    if (io.flux_out && io.flux_in) launch_plain_eo<T, K, DIFF, EO, 2>(s, io, md, Cp, L);
-    else if (io.flux_out) launch_plain_eo<T, K, DIFF, EO, 1>(s, io, md, Cp, L);
-    else launch_plain_eo<T, K, DIFF, EO, 0>(s, io, md, Cp, L);
+    if (io.flux_out && io.flux_in) {
+        if (io.pack) launch_plain_eo<T, K, DIFF, EO, 2, true>(s, io, md, Cp, L);
+        else launch_plain_eo<T, K, DIFF, EO, 2>(s, io, md, Cp, L);
+    } else if (io.flux_out) {
+        launch_plain_eo<T, K, DIFF, EO, 1>(s, io, md, Cp, L);
+    } else {
+        launch_plain_eo<T, K, DIFF, EO, 0>(s, io, md, Cp, L);
+    }
 }
 
 template <typename T, int K, bool DIFF>
@@ -362,6 +370,12 @@ int Solver::rk_stage_fp64(int s_idx, double dt, double* rhs_only)
     if (fluxes) {
         io.flux_in = flux_valid ? d_flux[flux_cur] : nullptr;
         io.flux_out = d_flux[1 - flux_cur];
+    }
+    if (s_idx == 2 && !rhs_only && stage3_pack && io.flux_in && io.flux_out) {
+        io.pack = stage3_pack;
+        io.pack_map = grid_map(mesh);
+        io.pack_gsize = gsize();
+        stage3_packed = true;
     }
     if (p.eval_diff) dispatch_grad<double, false>(*this, io, md);
     dispatch_stage<double, false>(*this, io, md, rhs_only ? 4 : s_idx);
@@ -740,6 +754,46 @@ int Solver::get_state_async(double* drho, double* vel)
     return DG_OK;
 }
 
+// One step whose result is downloaded: in the FP64 path with advection the
+// last stage writes its output in host order into staging slot k as well (no
+// pack kernel), then the download runs on the copy-out stream; otherwise a
+// step and dg_get_state_async.
+int Solver::step_get_async(double dt, double* drho, double* vel)
+{
+    if (!device_view(drho) || !device_view(vel))
+        return fail(DG_ERR_INVALID, "dg_step_get_state_async: host buffers must be page-locked (pinned)");
+    int rc = ensure_async();
+    if (rc) return rc;
+    if (!(fp64() && d_flux[0])) {
+        rc = step(dt, 1);
+        return rc ? rc : get_state_async(drho, vel);
+    }
+    const int k = out_slot;
+    out_slot ^= 1;
+    const size_t n = gsize();
+    double* st = astage_out[k];
+    DG_CUDA(cudaStreamWaitEvent(stream, out_free[k], 0));  // the download that last read the slot
+    stage3_pack = st;
+    stage3_packed = false;
+    rc = step(dt, 1);
+    stage3_pack = nullptr;
+    if (rc) return rc;
+    if (!stage3_packed) {
+        // the last stage ran in a mode without the pack: pack separately
+        const GridMap g = grid_map(mesh);
+        pack_host_order_kernel<double><<<152 * 16, 128, 0, stream>>>((const double*)state_ptr(), mesh.fstride(),
+                                                                     mesh.NP, g, st, st + n, n);
+        launches++;
+        DG_CUDA(cudaGetLastError());
+    }
+    DG_CUDA(cudaEventRecord(out_ready[k], stream));
+    DG_CUDA(cudaStreamWaitEvent(copy_out, out_ready[k], 0));
+    DG_CUDA(cudaMemcpyAsync(drho, st, n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
+    DG_CUDA(cudaMemcpyAsync(vel, st + n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, copy_out));
+    DG_CUDA(cudaEventRecord(out_free[k], copy_out));
+    return DG_OK;
+}
+
 int Solver::sync_all()
 {
     DG_CUDA(cudaStreamSynchronize(stream));
@@ -981,6 +1035,13 @@ int dg_set_state_async(dg_handle* h, const double* drho, const double* vel)
 {
     if (!h || !drho || !vel) return fail(DG_ERR_INVALID, "dg_set_state_async: null argument");
     return h->s.set_state_async(drho, vel);
+}
+
+int dg_step_get_state_async(dg_handle* h, double dt, double* drho, double* vel)
+{
+    if (!h || !drho || !vel) return fail(DG_ERR_INVALID, "dg_step_get_state_async: null argument");
+    if (!std::isfinite(dt)) return fail(DG_ERR_INVALID, "dg_step_get_state_async: bad dt");
+    return h->s.step_get_async(dt, drho, vel);
 }
 
 int dg_get_state_async(dg_handle* h, double* drho, double* vel)

@@ -128,6 +128,9 @@ struct Solver {
     int ensure_async();
     int set_state_async(const double* drho, const double* vel);
     int get_state_async(double* drho, double* vel);
+    int step_get_async(double dt, double* drho, double* vel);
+    double* stage3_pack = nullptr;  // set by step_get_async: the last stage also packs its output here
+    bool stage3_packed = false;      // it did
     int sync_all();
     ~Solver();
 };

@@ -131,6 +131,13 @@ int dg_set_state(dg_handle* h, const double* drho, const double* vel);
  * Pageable buffers are rejected with DG_ERR_INVALID. */
 int dg_set_state_async(dg_handle* h, const double* drho, const double* vel);
 int dg_get_state_async(dg_handle* h, double* drho, double* vel);
+/* One RK step followed by dg_get_state_async of its result, in one call (no
+ * counterpart in the reference).  In the FP64 path with advection the step's
+ * last stage writes its output in host order into the download staging as it
+ * writes the state, so no separate pack runs; the bytes are those of dg_step
+ * then dg_get_state_async.  Otherwise it is exactly those two calls.  Host
+ * buffers: as dg_get_state_async (pinned, unread until dg_synchronize). */
+int dg_step_get_state_async(dg_handle* h, double dt, double* drho, double* vel);
 
 /* One evaluation R = L(u) of the semi-discrete right-hand side at the current
  * state (LDG diffusion, advection, sponge; no RK combination) into host

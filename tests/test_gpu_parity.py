@@ -539,3 +539,44 @@ def test_async_uploads_back_to_back(precision, advect, solver_for):
     ra, va = a.state()
     rb, vb = b.state()
     assert np.array_equal(ra, rb) and np.array_equal(va, vb)
+
+
+@pytest.mark.parametrize("order,precision,advect,nb", [(3, 64, 1, (1, 1, 1)), (4, 64, 1, (2, 1, 2)),
+                                                        (4, 64, 0, (1, 1, 1)), (3, 32, 1, (1, 1, 1))])
+def test_step_and_download_matches_separate_calls(order, precision, advect, nb, solver_for):
+    """dg_step_get_state_async (in the FP64 path with advection the last stage
+    writes the host-order download itself) gives the bytes of dg_step followed
+    by a download, through uploads, and leaves the state the same."""
+    import torch
+    cfg = small(order=order, ne=(2, 3, 4))
+    cfg["NUM_BLOCKS"] = list(nb)
+    cfg["PRECISION"] = precision
+    cfg["EVALUATE_ADVECTION"] = advect
+    a, b = solver_for(cfg), solver_for(cfg)
+    shape = a.dims
+    rng = np.random.default_rng(order + 7)
+
+    def pinned(shp):
+        return torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
+
+    ins = []
+    for _ in range(3):
+        r, v = pinned(shape), pinned((3,) + shape)
+        r[...] = rng.standard_normal(shape) * 1e-3
+        v[...] = rng.standard_normal((3,) + shape) * 1e-6
+        ins.append((r, v))
+    outs = [(pinned(shape), pinned((3,) + shape)) for _ in range(3)]
+    for k in range(3):
+        a.set_state_async(*ins[k])
+        a.step(cfg["DT"], 1)
+        a.step_state_async(cfg["DT"], *outs[k])
+    a.synchronize()
+    for k in range(3):
+        b.set_state(*ins[k])
+        b.step(cfg["DT"], 2)
+        r, v = b.state()
+        assert np.max(np.abs(r)) > 0
+        assert np.array_equal(r, outs[k][0]) and np.array_equal(v, outs[k][1]), k
+    ra, va = a.state()
+    rb, vb = b.state()
+    assert np.array_equal(ra, rb) and np.array_equal(va, vb)
