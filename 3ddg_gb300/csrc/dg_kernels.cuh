@@ -617,9 +617,11 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 // FP64 LDG gradient with even-odd line owners (K = 5: eo_lines): two
 // elements per CTA so that the 3 K^2 line tasks of each pack densely into
 // warps; each owner loads the neighbour values at its line's two ends, forms
-// the central face sums, and applies the even-odd operator.  One barrier
-// after the element's values reach shared memory, one before the coalesced
-// stores.
+// the central face sums, applies the even-odd operator and stores its line's
+// K results of G_a itself (every value of G has exactly one owner), so the
+// kernel has one barrier, after the element's values reach shared memory,
+// and the threads without a line leave at it.  The stores along y- and
+// z-lines are strided; the kernel is bound by the FP64 pipe, not by memory.
 template <int K>
 __host__ __device__ constexpr bool eo_lines()
 {
@@ -627,8 +629,8 @@ __host__ __device__ constexpr bool eo_lines()
 }
 
 template <int K>
-__device__ __forceinline__ void grad_eo_line(const LineEOAxis<K>& X, GradSmem<double, K>& S, int a, int t,
-                                             const double ro[2])
+__device__ __forceinline__ void grad_eo_line(const LineEOAxis<K>& X, const GradSmem<double, K>& S, int a, int t,
+                                             const double ro[2], double* __restrict__ q_elem)
 {
     const int st = axis_stride<K>(a);
     const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K * K + t / K : t * K);
@@ -637,7 +639,7 @@ __device__ __forceinline__ void grad_eo_line(const LineEOAxis<K>& X, GradSmem<do
     for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
     eo_apply<K, -1>(X, v, ro[0] + v[0], ro[1] + v[K - 1], out);  // flux factors are in the lift columns
 #pragma unroll
-    for (int i = 0; i < K; i++) S.out[a][b0 + i * st] = out[i];
+    for (int i = 0; i < K; i++) q_elem[b0 + i * st] = out[i];
 }
 
 template <int K>
@@ -664,12 +666,7 @@ ldg_gradient_eo_kernel(StageIO<double> io, MeshDev<double> m, const OpConst<doub
     if (owner) line_end_values<false, false, false, double, K>(io, m, C, el, la, t, ro, unused_u, unused_q);
     sm_all[threadIdx.y].r[n] = rho;
     __syncthreads();
-    if (owner) grad_eo_line<K>(eo[la], sm_all[le], la, t, ro);
-    __syncthreads();
-    if (!act) return;
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-        io.q_out[(size_t)a * io.fs + (size_t)e * io.np + n] = sm_all[threadIdx.y].out[a][n];
+    if (owner) grad_eo_line<K>(eo[la], sm_all[le], la, t, ro, io.q_out + (size_t)la * io.fs + (size_t)el * io.np);
 }
 
 // Shared memory of a stage kernel, per element: for each axis a, the pair
