@@ -117,17 +117,26 @@ __device__ __forceinline__ void batch_end_codes(const BatchProblem& P, const Bat
     code[1] = live ? __ldg(P.nbr + (size_t)e * 6 + 2 * a + 1) : 0;
 }
 
+// Shared memory of the gradient phase, per element slot: drho of every node,
+// double-buffered by pass parity.
+template <int K>
+struct BatchGradSmem {
+    float r[2][npt_of(K)];
+};
+
 // The gradient phase of one tile.  Each line owner loads the neighbour
-// values at its line's two ends and forms the two central face fluxes itself
-// (the values the face-node form staged in shared memory), so a pass has two
-// barriers; the owners' face-table codes of each pass are loaded during the
-// pass before.
+// values at its line's two ends, forms the two central face fluxes itself
+// and stores its line's results (every value of the gradient has one owner),
+// so a pass has one barrier: with drho double-buffered, a pass's writes go
+// to the buffer the pass before last read, which every owner finished before
+// the previous pass's barrier.  The owners' face-table codes of each pass
+// are loaded during the pass before.
 template <int K>
 __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, const BatchTile& T, int stage,
                                 unsigned char* smraw)
 {
     constexpr int K2 = K * K, K3 = K * K * K, NPT = npt_of(K), EPB = bepb_of(K);
-    GradSmem<float, K>* SM = reinterpret_cast<GradSmem<float, K>*>(smraw);
+    BatchGradSmem<K>* SM = reinterpret_cast<BatchGradSmem<K>*>(smraw);
     const int slot = threadIdx.x / NPT, n = threadIdx.x % NPT;
     const float* ub = P.u[P.cur];
     const float* inc = stage == 0 ? nullptr : P.d[stage - 1];
@@ -137,7 +146,8 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
     const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K2 + (t / K) : t * K);
     int code_next[2];
     batch_end_codes<K>(P, T, T.e0, task, ls, a, code_next);
-    for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB) {
+    int buf = 0;
+    for (int c0 = T.e0; c0 < T.e0 + T.count; c0 += EPB, buf ^= 1) {
         const int e = c0 + slot;
         const bool act = slot < EPB && e < T.e0 + T.count && n < K3;
         const bool owner = task && c0 + ls < T.e0 + T.count;
@@ -159,13 +169,14 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
                 }
             }
         }
-        if (slot < EPB) SM[slot].r[n] = rho;
+        if (slot < EPB) SM[slot].r[buf][n] = rho;
         __syncthreads();
         if (owner) {
-            GradSmem<float, K>& S = SM[ls];
+            const float* r = SM[ls].r[buf];
+            float* q = P.q + (size_t)a * P.fs + (size_t)(c0 + ls) * P.np;
             float v[K];
 #pragma unroll
-            for (int j = 0; j < K; j++) v[j] = S.r[b0 + j * st];
+            for (int j = 0; j < K; j++) v[j] = r[b0 + j * st];
             const float f0 = 0.5f * (ro[0] + v[0]), fN = -0.5f * (ro[1] + v[K - 1]);
             const float gs = P.gscale[a];
 #pragma unroll
@@ -175,16 +186,9 @@ __device__ void batch_grad_tile(const BatchProblem& P, const BatchOps& ops, cons
                 s2 += row[K + 1] * fN;
 #pragma unroll
                 for (int j = 0; j < K; j++) s2 += row[j] * v[j];
-                S.out[a][b0 + i * st] = gs * s2;
+                q[b0 + i * st] = gs * s2;
             }
         }
-        __syncthreads();
-        // no barrier before the next pass: it writes S.r (read above before
-        // the second barrier) and S.out only after its first barrier, which
-        // every thread reaches after these reads
-        if (act)
-#pragma unroll
-            for (int a2 = 0; a2 < 3; a2++) P.q[(size_t)a2 * P.fs + (size_t)e * P.np + n] = SM[slot].out[a2][n];
     }
 }
 
@@ -363,11 +367,11 @@ __device__ void batch_stage_tile(const BatchProblem& P, const BatchOps& ops, con
     }
 }
 
-// Shared memory of one CTA of order K.
-template <int K>
+// Shared memory of one CTA of order K in phase PHASE.
+template <int K, int PHASE>
 __host__ __device__ constexpr size_t batch_smem_bytes()
 {
-    return bepb_of(K) * sizeof(PlainSmem<float, K>);
+    return bepb_of(K) * (PHASE == 0 ? sizeof(BatchGradSmem<K>) : sizeof(PlainSmem<float, K>));
 }
 
 // Resident CTAs per SM asked of the compiler for the gradient phase (register
@@ -407,7 +411,7 @@ template <int K, int PHASE>
 __global__ void __launch_bounds__(bthreads_of(K), batch_min_blocks(K, PHASE))
     batch_stage_kernel(BatchArgs A, const BatchOps ops)
 {
-    __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K>()];
+    __shared__ __align__(16) unsigned char smraw[batch_smem_bytes<K, PHASE>()];
     __shared__ BatchProblem P;
     __shared__ int tile_idx;
     for (;;) {

@@ -220,7 +220,6 @@ template <typename T, int K>
 struct GradSmem {
     T r[npt_of(K)];
     T fl[3][2][K * K];
-    T out[3][npt_of(K)];  // line-owner results (FP32, K >= 5)
 };
 
 template <bool INCR, typename T>
@@ -464,9 +463,11 @@ __device__ __forceinline__ void stage_line_faces(const OpConst<T, K>& Cv, Smem& 
     }
 }
 
-// The same for the LDG gradient: central flux of drho at both ends.
+// The same for the LDG gradient: central flux of drho at both ends; the
+// owner stores its line's K values of G_A at q_elem (the element's G_A).
 template <int A, typename T, int K, typename Smem>
-__device__ __forceinline__ void grad_line_faces(const OpConst<T, K>& Cv, Smem& S, int t, const T ro[2])
+__device__ __forceinline__ void grad_line_faces(const OpConst<T, K>& Cv, const Smem& S, int t, const T ro[2],
+                                                T* __restrict__ q_elem)
 {
     constexpr int st = axis_stride<K>(A);
     const int b0 = line_base<A, K>(t);
@@ -481,7 +482,7 @@ __device__ __forceinline__ void grad_line_faces(const OpConst<T, K>& Cv, Smem& S
         s2 += row[K + 1] * fN;
 #pragma unroll
         for (int j = 0; j < K; j++) s2 += row[j] * v[j];
-        S.out[A][b0 + i * st] = s2;
+        q_elem[b0 + i * st] = s2;
     }
 }
 
@@ -540,7 +541,8 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     const bool act = n < K3 && live;
     const int c[3] = {n / K2, (n / K) % K, n % K};
     if constexpr (LINES) {
-        // Line owners with their own face terms: one barrier per element.
+        // Line owners with their own face terms, storing their lines' results
+        // themselves (every value of G has one owner): one barrier per element.
         constexpr int WPA = (K2 + 31) / 32;
         const int w = n / 32, a = w / WPA, t = (w % WPA) * 32 + n % 32;
         const bool owner = live && a < 3 && t < K2;
@@ -550,14 +552,11 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
         S.r[n] = rho;
         __syncthreads();
         if (owner) {
-            if (a == 0) grad_line_faces<0>(Cv, S, t, ro);
-            else if (a == 1) grad_line_faces<1>(Cv, S, t, ro);
-            else grad_line_faces<2>(Cv, S, t, ro);
+            T* q = io.q_out + (size_t)a * io.fs + (size_t)e * io.np;
+            if (a == 0) grad_line_faces<0>(Cv, S, t, ro, q);
+            else if (a == 1) grad_line_faces<1>(Cv, S, t, ro, q);
+            else grad_line_faces<2>(Cv, S, t, ro, q);
         }
-        __syncthreads();
-        if (!act) return;
-#pragma unroll
-        for (int a2 = 0; a2 < 3; a2++) io.q_out[(size_t)a2 * io.fs + (size_t)e * io.np + n] = S.out[a2][n];
     } else {
         // Face nodes assigned densely (see stage_kernel): their neighbour (or
         // exterior) values are loaded with the thread's own node.
