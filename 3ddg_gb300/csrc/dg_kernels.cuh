@@ -711,9 +711,11 @@ __host__ __device__ constexpr int plain_min_blocks()
 // One line of an FP64 stage kernel with even-odd line owners: the mass
 // equation's line (flux f_mass + G, face terms gr) into S.m and the momentum
 // equation's (f_mom, gm) into S.q, along runtime axis a.
+// The line's face terms g0 (first node) and gN (last node) come from its
+// owner (x momentum, y density).
 template <int K>
 __device__ __forceinline__ void stage_eo_line(const LineEOAxis<K>& X, PlainSmem<double, K>& S, int a, int t,
-                                              int do_adv)
+                                              int do_adv, const double2 g0, const double2 gN)
 {
     const int st = axis_stride<K>(a);
     const int b0 = a == 0 ? t : (a == 1 ? (t % K) * K * K + t / K : t * K);
@@ -721,16 +723,42 @@ __device__ __forceinline__ void stage_eo_line(const LineEOAxis<K>& X, PlainSmem<
     double v[K], out[K];
 #pragma unroll
     for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st].y;
-    eo_apply<K, 1>(X, v, S.g[a][0][t].y, S.g[a][1][t].y, out);
+    eo_apply<K, 1>(X, v, g0.y, gN.y, out);
 #pragma unroll
     for (int i = 0; i < K; i++) S.m[a][b0 + i * st] = out[i];
     if (do_adv) {
 #pragma unroll
         for (int j = 0; j < K; j++) v[j] = S.f[a][b0 + j * st].x;
-        eo_apply<K, 1>(X, v, S.g[a][0][t].x, S.g[a][1][t].x, out);
+        eo_apply<K, 1>(X, v, g0.x, gN.x, out);
 #pragma unroll
         for (int i = 0; i < K; i++) S.q[a][b0 + i * st] = out[i];
     }
+}
+
+// Face term (x momentum, y density) of face node nf of an element on axis a,
+// side ``side``: the numerical flux (impedance upwind for advection, central
+// for LDG) times its lift scale, from the element's own values in shared
+// memory and the neighbour (or exterior) values ro, uo (drho and the normal
+// velocity, or in flux mode 2 their momentum and mass fluxes) and qo.
+template <typename T, int K, bool DIFF, int FLUX>
+__device__ __forceinline__ typename Pair<T>::type face_term(const OpConst<T, K>& C, const PlainSmem<T, K>& S,
+                                                            int a, int side, int nf, T ro, T uo, T qo, int do_adv)
+{
+    const T fm_s = S.f[a][nf].x, fa_s = S.m[a][nf];
+    T gm = T(0), gr = T(0);
+    if (do_adv) {
+        const T fmo = FLUX == 2 ? ro : momentum_flux(ro, C.k1, C.k2);
+        const T fao = FLUX == 2 ? uo : mass_flux(uo, ro, C.r0, C.linear_mass);
+        const T* cm = C.cM[a][side];
+        const T* cr = C.cA[a][side];
+        gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
+        gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
+    }
+    if (DIFF) gr += C.cQ[a][side] * (qo + S.q[a][nf]);
+    typename Pair<T>::type g;
+    g.x = gm;
+    g.y = gr;
+    return g;
 }
 
 //
@@ -793,26 +821,51 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     }
     // Neighbour (or exterior) values of this thread's face nodes: drho and
     // the normal velocity, or in flux mode 2 their momentum and mass fluxes.
-    T ro[R], uo[R], qo[R];
+    // Per-node line sums: the element's 6 K^2 face nodes dealt out densely
+    // (slots n, n + NPT, ...).  EO: the two ends of this thread's line task
+    // (element le of the CTA, axis la, line lt), whose face terms its owner
+    // evaluates itself, so the face phase needs no barrier of its own.
+    constexpr int NL = 3 * K2, RF = EO ? 2 : R;
+    const int tid = threadIdx.y * NPT + n;
+    const int le = tid / NL, la = (tid % NL) / K2, lt = tid % K2;
+    const bool owner = EO && tid < EPB * NL && blockIdx.x * EPB + le < m.n_elem;
+    T ro[RF], uo[RF], qo[RF];
 #pragma unroll
-    for (int r = 0; r < R; r++) {
+    for (int r = 0; r < RF; r++) {
         ro[r] = uo[r] = qo[r] = T(0);
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        const int code = __ldg(m.nbr + (size_t)e * 6 + 2 * F.a + F.side);
+        int fa, fside, ffi, fnn, fe;
+        if constexpr (EO) {
+            if (!owner) continue;
+            const int st = axis_stride<K>(la);
+            const int b0 = la == 0 ? lt : (la == 1 ? (lt % K) * K2 + lt / K : lt * K);
+            fa = la;
+            fside = r;
+            ffi = lt;
+            fnn = b0 + (r ? 0 : (K - 1) * st);
+            fe = blockIdx.x * EPB + le;
+        } else {
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            fa = F.a;
+            fside = F.side;
+            ffi = F.fi;
+            fnn = F.nn;
+            fe = e;
+        }
+        const int code = __ldg(m.nbr + (size_t)fe * 6 + 2 * fa + fside);
         if (code >= 0) {
-            const size_t o2 = (size_t)code * io.np + F.nn;
+            const size_t o2 = (size_t)code * io.np + fnn;
             if (FLUX == 2) {
                 ro[r] = __ldg(io.flux_in + o2);
-                uo[r] = __ldg(io.flux_in + (size_t)(1 + F.a) * io.fs + o2);
+                uo[r] = __ldg(io.flux_in + (size_t)(1 + fa) * io.fs + o2);
             } else {
                 ro[r] = load_in<false>(io, 0, o2);
-                uo[r] = load_in<false>(io, 1 + F.a, o2);
+                uo[r] = load_in<false>(io, 1 + fa, o2);
             }
-            if (DIFF) qo[r] = __ldg(io.q + (size_t)F.a * io.fs + o2);
+            if (DIFF) qo[r] = __ldg(io.q + (size_t)fa * io.fs + o2);
         } else {
-            exterior<T, K>(m, C, -1 - code, F.side, F.fi, ro[r], uo[r]);
+            exterior<T, K>(m, C, -1 - code, fside, ffi, ro[r], uo[r]);
             if (FLUX == 2) {
                 const T fm = momentum_flux(ro[r], C.k1, C.k2);
                 uo[r] = mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
@@ -840,36 +893,30 @@ stage_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict__ Cp, 
     }
     __syncthreads();
 
-    // Face terms: the numerical flux (impedance upwind for advection, central
-    // for LDG) times its lift scale.
+    // Face terms (dense form): the numerical flux times its lift scale.
+    if constexpr (!EO) {
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = n + r * NPT;
-        if (!live || t >= NF) continue;
-        const FaceNode<K> F(t);
-        const T fm_s = S.f[F.a][F.nf].x, fa_s = S.m[F.a][F.nf];
-        T gm = T(0), gr = T(0);
-        if (do_adv) {
-            const T fmo = FLUX == 2 ? ro[r] : momentum_flux(ro[r], C.k1, C.k2);
-            const T fao = FLUX == 2 ? uo[r] : mass_flux(uo[r], ro[r], C.r0, C.linear_mass);
-            const T* cm = C.cM[F.a][F.side];
-            const T* cr = C.cA[F.a][F.side];
-            gm = fmo * cm[0] + fm_s * cm[1] + fao * cm[2] + fa_s * cm[3];
-            gr = fmo * cr[0] + fm_s * cr[1] + fao * cr[2] + fa_s * cr[3];
+        for (int r = 0; r < R; r++) {
+            const int t = n + r * NPT;
+            if (!live || t >= NF) continue;
+            const FaceNode<K> F(t);
+            S.g[F.a][F.side][F.fi] = face_term<T, K, DIFF, FLUX>(C, S, F.a, F.side, F.nf, ro[r], uo[r], qo[r], do_adv);
         }
-        if (DIFF) gr += C.cQ[F.a][F.side] * (qo[r] + S.q[F.a][F.nf]);
-        S.g[F.a][F.side][F.fi].x = gm;
-        S.g[F.a][F.side][F.fi].y = gr;
+        __syncthreads();
     }
-    __syncthreads();
 
     T r_rho = T(0), r_u[3] = {T(0), T(0), T(0)};
     if constexpr (EO) {
-        constexpr int NL = 3 * K2;
         static_assert(NL <= NPT, "line tasks must fit the element's threads");
-        const int tid = threadIdx.y * NPT + n;
-        const int le = tid / NL, la = (tid % NL) / K2, t = tid % K2;
-        if (tid < EPB * NL && blockIdx.x * EPB + le < m.n_elem) stage_eo_line<K>(eo[la], sm_all[le], la, t, do_adv);
+        if (owner) {
+            PlainSmem<T, K>& SL = sm_all[le];
+            const int st = axis_stride<K>(la);
+            const int b0 = la == 0 ? lt : (la == 1 ? (lt % K) * K2 + lt / K : lt * K);
+            const typename Pair<T>::type g0 = face_term<T, K, DIFF, FLUX>(C, SL, la, 0, b0, ro[0], uo[0], qo[0], do_adv);
+            const typename Pair<T>::type gN =
+                face_term<T, K, DIFF, FLUX>(C, SL, la, 1, b0 + (K - 1) * st, ro[1], uo[1], qo[1], do_adv);
+            stage_eo_line<K>(eo[la], SL, la, lt, do_adv, g0, gN);
+        }
         __syncthreads();
         if (!act) return;
         r_rho = S.m[0][n] + S.m[1][n];
