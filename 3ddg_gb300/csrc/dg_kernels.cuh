@@ -613,7 +613,7 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
     }
 }
 
-// FP64 LDG gradient with even-odd line owners (K = 5: eo_lines): two
+// FP64 LDG gradient with even-odd line owners (K = 4, 5: eo_grad_lines): two
 // elements per CTA so that the 3 K^2 line tasks of each pack densely into
 // warps; each owner loads the neighbour values at its line's two ends, forms
 // the central face sums, applies the even-odd operator and stores its line's
@@ -624,7 +624,16 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 template <int K>
 __host__ __device__ constexpr bool eo_lines()
 {
-    return K == 5;  // at K = 4 and K = 6 they measured no faster than per-node sums
+    return K == 5;  // stage kernel: at K = 4 (3.891 against 3.845 ms) and K = 6 no faster than per-node sums
+}
+
+// The same choice for the gradient kernel: at K = 4 its even-odd owners are
+// faster (1.106 against 1.122 ms per launch on 80^3 elements) where the stage
+// kernel's are not.
+template <int K>
+__host__ __device__ constexpr bool eo_grad_lines()
+{
+    return K == 4 || K == 5;
 }
 
 template <int K>

@@ -140,7 +140,7 @@ void launch_grad(Solver& s, const StageIO<T>& io, const MeshDev<T>& md)
     cudaEvent_t ev = nullptr;
     s.prof_begin(1, &ev);
     bool done = false;
-    if constexpr (!INCR && sizeof(T) == 8 && eo_lines<K>()) {
+    if constexpr (!INCR && sizeof(T) == 8 && eo_grad_lines<K>()) {
         LineEO<K> L;
         if (make_line_eo<K, -1>(host_const<T, K>(s, 3), L)) {
             ldg_gradient_eo_kernel<K><<<(md.n_elem + 1) / 2, dim3(npt_of(K), 2), 0, s.stream>>>(

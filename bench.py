@@ -426,7 +426,8 @@ def run_ours(a, dist: Dist):
                                   "flops counted by the direct formula (K (K + 2) per line), which the even-odd "
                                   "line owners execute with about 22 % fewer FP64 instructions"},
             "share_of_step": st_ms / ms if ms else None,
-            "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<5>" if fp64 and cfg["ORDER"] == 4 else
+            "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<%d>" % (cfg["ORDER"] + 1)
+                                         if fp64 and cfg["ORDER"] in (3, 4) else
                                          ("ldg_gradient_kernel<double,%d>" if fp64 else "ldg_gradient_kernel<float,%d>")
                                          % (cfg["ORDER"] + 1)),
                                 "launches": gr_n, "mean_launch_ms": gr_ms / gr_n if gr_n else None,
