@@ -621,19 +621,24 @@ ldg_gradient_kernel(StageIO<T> io, MeshDev<T> m, const OpConst<T, K>* __restrict
 // kernel has one barrier, after the element's values reach shared memory,
 // and the threads without a line leave at it.  The stores along y- and
 // z-lines are strided; the kernel is bound by the FP64 pipe, not by memory.
+// Orders whose FP64 stage kernel uses even-odd line owners, by measurement on
+// ~32.8 M nodes of config 2's physics (ms per launch, owners against per-node
+// sums): K = 2: 8.99 / 11.71 (the per-node form leaves 24 of a warp slice's
+// 32 lanes idle); K = 3: 4.49 / 4.57; K = 4: 3.891 / 3.845 (slower); K = 5:
+// 3.85 / 4.12; K = 6 no faster (448-thread CTAs at 92 registers).
 template <int K>
 __host__ __device__ constexpr bool eo_lines()
 {
-    return K == 5;  // stage kernel: at K = 4 (3.891 against 3.845 ms) and K = 6 no faster than per-node sums
+    return K <= 3 || K == 5;
 }
 
-// The same choice for the gradient kernel: at K = 4 its even-odd owners are
-// faster (1.106 against 1.122 ms per launch on 80^3 elements) where the stage
-// kernel's are not.
+// The same choice for the gradient kernel (ms per launch): K = 2: 1.54 /
+// 2.94; K = 3: 1.100 / 1.153; K = 4: 1.106 / 1.122; K = 5: 1.11 / 1.31;
+// K = 6, 7, 8 slower (1.59 / 1.40, 1.73 / 1.60, 2.48 / 1.68).
 template <int K>
 __host__ __device__ constexpr bool eo_grad_lines()
 {
-    return K == 4 || K == 5;
+    return K <= 5;
 }
 
 template <int K>
