@@ -169,6 +169,12 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- helpers
+# Orders N whose FP64 stage / gradient kernels use even-odd line owners (K = N + 1;
+# eo_lines and eo_grad_lines in 3ddg_gb300/csrc/dg_kernels.cuh), for the kernel labels.
+EO_STAGE_ORDERS = (1, 2, 4)
+EO_GRAD_ORDERS = (1, 2, 3, 4)
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -411,7 +417,8 @@ def run_ours(a, dist: Dist):
     roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
             "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s",
-            "kernel": (("stage_kernel<double,5,DIFF,2,EO> (fluxes read, even-odd line owners)" if cfg["ORDER"] == 4
+            "kernel": (("stage_kernel<double,%d,DIFF,2,EO> (fluxes read, even-odd line owners)" % (cfg["ORDER"] + 1)
+                        if cfg["ORDER"] in EO_STAGE_ORDERS
                         else "stage_kernel<double,%d,DIFF,2> (fluxes read, per-node line sums)" % (cfg["ORDER"] + 1))
                        if fp64 else "incr_stage_kernel<float,%d,DIFF>" % (cfg["ORDER"] + 1)),
             "algorithmic_bytes_per_launch": st_b / st_n if st_n else None,
@@ -427,7 +434,7 @@ def run_ours(a, dist: Dist):
                                   "line owners execute with about 22 % fewer FP64 instructions"},
             "share_of_step": st_ms / ms if ms else None,
             "gradient_kernel": {"name": ("ldg_gradient_eo_kernel<%d>" % (cfg["ORDER"] + 1)
-                                         if fp64 and cfg["ORDER"] in (3, 4) else
+                                         if fp64 and cfg["ORDER"] in EO_GRAD_ORDERS else
                                          ("ldg_gradient_kernel<double,%d>" if fp64 else "ldg_gradient_kernel<float,%d>")
                                          % (cfg["ORDER"] + 1)),
                                 "launches": gr_n, "mean_launch_ms": gr_ms / gr_n if gr_n else None,
