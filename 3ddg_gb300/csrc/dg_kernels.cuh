@@ -699,12 +699,14 @@ struct PlainSmem {
 // One RK stage of the plain (FP64) form: R = L(stage input), then the stage
 // combination dst = R' + s (cb - ca sigma) + cc old.
 //
-// The FP64 pipe is the bound, so the face fluxes are assigned densely: thread
-// n of an element evaluates face nodes n, n + NPT, ... of its 6 K^2, reading
-// the element's own values from shared memory.  (A thread per node evaluating
+// The FP64 pipe is the bound, so the face fluxes are assigned densely: with
+// per-node line sums, thread n of an element evaluates face nodes n, n + NPT,
+// ... of its 6 K^2, reading the element's own values from shared memory; with
+// even-odd line owners, each owner evaluates the two face nodes that end its
+// line (the line tasks are packed densely too).  (A thread per node evaluating
 // its own faces would issue every axis's face arithmetic in nearly every warp,
-// since almost every warp holds some node on each face pair.)  The
-// neighbour values of those face nodes are loaded with the thread's own node.
+// since almost every warp holds some node on each face pair.)  The neighbour
+// values of those face nodes are loaded with the thread's own node.
 // ---------------------------------------------------------------------------
 // Elements per CTA of the FP64 stage kernel: two with even-odd line owners
 // (EO), so that the 3 K^2 line tasks of each pack densely into warps.
