@@ -202,3 +202,15 @@ def test_hdf5_bad_path_is_reference_error_code(tmp_path):
     m = dg()
     with pytest.raises(m.DGError, match=r"\(-1\).*FileIException"):
         m.hdf5_write(str(tmp_path / "no" / "such" / "dir.h5"), "rho", np.zeros((2, 2, 2)))
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No fallback: with libdg3d.so absent, the first call raises DGError
+    instead of running anything else."""
+    m = dg()
+    monkeypatch.setattr(m, "LIB_PATH", str(tmp_path / "libdg3d.so"))
+    monkeypatch.setattr(m, "_lib", None)
+    with pytest.raises(m.DGError, match="not built"):
+        m.lib()
+    with pytest.raises(m.DGError):
+        m.Solver(workloads().config1(seed=0))
