@@ -582,27 +582,31 @@ def test_step_and_download_matches_separate_calls(order, precision, advect, nb, 
     assert np.array_equal(ra, rb) and np.array_equal(va, vb)
 
 
-@pytest.mark.parametrize("order", [2, 3, 4])
-def test_rhs_is_mirror_symmetric_in_x(order, solver_for):
+@pytest.mark.parametrize("order,axis", [(2, 0), (3, 0), (4, 0), (4, 1), (4, 2), (3, 2)])
+def test_rhs_is_mirror_symmetric(order, axis, solver_for):
     """The GPU right-hand side (nonlinear flux, LDG diffusion, sponge on all
-    faces, mesh centred on x = 0) commutes with the reflection x -> -x of
-    the node grid with u_x -> -u_x: a check of every face coefficient's and
-    lift column's orientation along x that does not go through the oracle
-    (orders 2 and 4 use the even-odd line owners, 3 the per-node sums)."""
+    faces, mesh centred on the origin) commutes with the reflection of the
+    node grid along each axis, the normal velocity changing sign: a check of
+    every face coefficient's and lift column's orientation that does not go
+    through the oracle (orders 2 and 4 use the even-odd line owners, 3 the
+    per-node sums in the stage kernel)."""
     cfg = small(order=order, ne=(4, 3, 2))
     s = solver_for(cfg)
     X, Y, Z = s.dims
-    rng = np.random.default_rng(20 + order)
+    rng = np.random.default_rng(20 + order + 3 * axis)
     rho = rng.standard_normal((X, Y, Z)) * 1e-3
     vel = rng.standard_normal((3, X, Y, Z)) * 1e-6
+
+    def mirror(a, b):
+        am, bm = np.flip(a, axis).copy(), np.flip(b, axis + 1).copy()
+        bm[axis] *= -1.0
+        return am, bm
+
     s.set_state(rho, vel)
     r, v = s.rhs()
-    vel_m = vel[:, ::-1].copy()
-    vel_m[0] *= -1.0
-    s.set_state(rho[::-1].copy(), vel_m)
+    s.set_state(*mirror(rho, vel))
     rm, vm = s.rhs()
-    want_v = v[:, ::-1].copy()
-    want_v[0] *= -1.0
-    assert np.max(np.abs(rm - r[::-1])) <= 1e-12 * np.max(np.abs(r))
+    want_r, want_v = mirror(r, v)
+    assert np.max(np.abs(rm - want_r)) <= 1e-12 * np.max(np.abs(r))
     assert np.max(np.abs(vm - want_v)) <= 1e-12 * np.max(np.abs(v))
     assert np.max(np.abs(rm - r)) > 1e-3 * np.max(np.abs(r))

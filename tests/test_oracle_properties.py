@@ -1,11 +1,11 @@
 """Size-independent properties of the C oracle's right-hand side, beside its
 pin to the reference's golden vectors (tests/test_oracle_golden.py): the
 operator is affine in the state when the flux is linear (B/A = 0; diffusion
-and sponge are linear), and the equations are symmetric under the mirror
-x -> -x of a mesh and sponge symmetric about x = 0 (with u_x -> -u_x), for
-the full nonlinear, diffusive, sponged operator.  The mirror case checks the
-orientation of every face coefficient and lift column along x
-(cppsrc/Element.cpp:542-600).  CPU only."""
+and sponge are linear), and the equations are symmetric under the mirror of
+a mesh and sponges symmetric about the origin along each axis (with the
+normal velocity changing sign), for the full nonlinear, diffusive, sponged
+operator.  The mirror cases check the orientation of every face coefficient
+and lift column along each axis (cppsrc/Element.cpp:542-600).  CPU only."""
 import os
 
 import numpy as np
@@ -64,21 +64,29 @@ def test_rhs_is_affine_with_linear_flux(order):
     o.close()
 
 
-@pytest.mark.parametrize("order", [2, 3])
-def test_rhs_is_mirror_symmetric_in_x(order):
-    """Sponge widths [1, 1, ...] on -X and +X, a mesh centred on x = 0: the
-    operator commutes with the reflection of the node grid in x."""
-    o = oracle(base_cfg(order, (4, 2, 3), 5.0))
-    rng = np.random.default_rng(10 + order)
+def mirror(rho, vel, axis):
+    """Reflection of the node grid along ``axis`` (LGL nodes are symmetric,
+    so node i of the grid maps to node X - 1 - i), the normal velocity
+    component changing sign."""
+    rho_m = np.flip(rho, axis).copy()
+    vel_m = np.flip(vel, axis + 1).copy()
+    vel_m[axis] *= -1.0
+    return rho_m, vel_m
+
+
+@pytest.mark.parametrize("order,axis", [(2, 0), (3, 0), (3, 1), (2, 2), (4, 1)])
+def test_rhs_is_mirror_symmetric(order, axis):
+    """Sponges of one element on all six faces, a mesh centred on the origin:
+    the operator commutes with the reflection of the node grid along each
+    axis."""
+    cfg = base_cfg(order, (4, 2, 3), 5.0)
+    cfg["BC_SPONGE_WIDTH"] = [1] * 6
+    o = oracle(cfg)
+    rng = np.random.default_rng(10 + order + 3 * axis)
     rho, vel = random_state(o, rng)
-    rho_m = rho[::-1].copy()
-    vel_m = vel[:, ::-1].copy()
-    vel_m[0] *= -1.0
     r, v = rhs_of(o, rho, vel)
-    rm, vm = rhs_of(o, rho_m, vel_m)
-    want_r = r[::-1]
-    want_v = v[:, ::-1].copy()
-    want_v[0] *= -1.0
+    rm, vm = rhs_of(o, *mirror(rho, vel, axis))
+    want_r, want_v = mirror(r, v, axis)
     assert np.max(np.abs(rm - want_r)) <= 1e-12 * np.max(np.abs(r))
     assert np.max(np.abs(vm - want_v)) <= 1e-12 * np.max(np.abs(v))
     # the check has teeth: the unmirrored state gives a different field
